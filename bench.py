@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Throughput of the hex convection + diffusion residuals (one JSON line).
+
+A step is one evaluation of both residuals -- full_convec_ijk then
+full_diffusion_ijk -- over the plain_64 workload: 64^3 hexes, porder 4
+(257^3 = 16,974,593 shared nodes), +-5% seeded vertex jitter, seeded Fourier
+fields (FP32).  value = 5 * npoin / (time per step) in GDOF/s: one
+degree of freedom per unique node and conserved variable (mass, 3 momentum,
+energy) for the full right-hand side.  Inputs (2.4 GB per call) exceed the
+129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N --steps K --warmup W]            this library on the GPU
+  python bench.py --impl reference [--steps K --warmup W]    the reference algorithm on the host cores
+
+Under torchrun each rank runs its own replica of the workload (weak scaling,
+no collective on the data path); rank 0 prints the max-over-ranks timing.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "convec+diffu GDOF/s & % HBM roofline; mixed/learned vs plain at stated error"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def algorithmic_bytes(nelem, n, npoin):
+    """Compulsory bytes per call: every input read once, every output written once."""
+    conv = nelem * n * (4 + 36 + 4) + npoin * (36 + 20)
+    diff = nelem * n * (4 + 36 + 4 + 4 + 4) + npoin * (24 + 20)
+    return conv, diff
+
+
+def peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            v = float(json.load(f)["hbm_gbs"])
+        return v, "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.strip()]
+        self.file.close()
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return rank, local, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def load_traffic(workload_name):
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary (or None)."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(workload_name)
+    except Exception:
+        return None
+
+
+# --------------------------------------------------------------------------------------
+# CPU legs: the oracle (restatement of the reference's CPU path) on a bounded sample
+# --------------------------------------------------------------------------------------
+def cpu_sample_case(cfg, host, nsample):
+    """A contiguous slab of `nsample` elements from the middle of the mesh with its
+    metric computed by the oracle's elem_jacobian."""
+    from oracle import oracle as O
+
+    n = cfg.nnode
+    e0 = max(0, host.nelem // 2 - nsample // 2)
+    e1 = min(host.nelem, e0 + nsample)
+    con = np.ascontiguousarray(host.connec.reshape(n, host.nelem)[:, e0:e1]).reshape(-1)
+    t = host.tables
+    He, gp = O.elem_jacobian(cfg.porder, e1 - e0, host.npoin, con, host.coord, t["dNgp"], t["wgp"])
+    geom = dict(t, connec=con, He=He, gpvol=gp)
+    mu = np.zeros((e1 - e0) * n, np.float32)
+    return geom, e1 - e0, mu
+
+
+def cpu_step(cfg, host, geom, ne, mu, nthreads):
+    from oracle import oracle as O
+
+    f = host.fields
+    O.full_convec_ijk(cfg.porder, ne, host.npoin, geom, f["u"], f["q"], f["rho"], f["pr"], f["E"],
+                      nthreads=nthreads)
+    O.full_diffusion_ijk(cfg.porder, ne, host.npoin, geom, cfg.Cp, cfg.Pr, f["rho"], f["u"], f["Tem"],
+                         f["mu_fluid"], mu, mu, nthreads=nthreads)
+
+
+def calibrate_sample(cfg, host, nthreads, seconds):
+    """Number of elements whose convec+diffu takes about `seconds` on `nthreads`."""
+    ne = 256 if nthreads == 1 else 256 * nthreads
+    geom, ne, mu = cpu_sample_case(cfg, host, ne)
+    t0 = time.perf_counter()
+    cpu_step(cfg, host, geom, ne, mu, nthreads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    want = int(ne * seconds / dt)
+    return max(64, min(host.nelem, want))
+
+
+def cpu_baseline(cfg, host, seconds=12.0):
+    """The serial oracle (the faithful single-core restatement) on a bounded sample."""
+    ns = calibrate_sample(cfg, host, 1, seconds)
+    geom, ne, mu = cpu_sample_case(cfg, host, ns)
+    t0 = time.perf_counter()
+    cpu_step(cfg, host, geom, ne, mu, 1)
+    dt = time.perf_counter() - t0
+    dofs = 5.0 * host.npoin * ne / host.nelem
+    return {"value": dofs / dt / 1e9, "unit": "GDOF/s", "cores": 1, "kind": "port",
+            "sample": "%d of %d elements (a contiguous slab), convec+diffu, serial oracle, %.1f s; DOFs "
+                      "prorated by element share" % (ne, host.nelem, dt)}
+
+
+def run_reference(args, cfg):
+    """--impl reference: the reference algorithm (the oracle port) on all host cores."""
+    from minisod2d_gb300 import workload
+    from oracle import oracle as O
+
+    O.lib()
+    host = workload.HostCase(cfg)
+    nth = O.cpu_count()
+    per_step = max(1.0, min(5.0, 90.0 / max(1, args.steps + args.warmup)))
+    ns = calibrate_sample(cfg, host, nth, per_step)
+    geom, ne, mu = cpu_sample_case(cfg, host, ns)
+    for _ in range(args.warmup):
+        cpu_step(cfg, host, geom, ne, mu, nth)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_step(cfg, host, geom, ne, mu, nth)
+    dt = (time.perf_counter() - t0) / max(1, args.steps)
+    dofs = 5.0 * host.npoin * ne / host.nelem
+    value = dofs / dt / 1e9
+    sample = ("%d of %d elements per step (a contiguous slab), convec+diffu, OpenMP oracle on %d threads; DOFs "
+              "prorated by element share" % (ne, host.nelem, nth))
+    out = {"metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+           "config": {"workload": cfg.name, "porder": cfg.porder, "nelem": host.nelem, "npoin": host.npoin,
+                      "parallelism": "host cores"},
+           "cpu_baseline": {"value": value, "unit": "GDOF/s", "cores": nth, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "GDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# --------------------------------------------------------------------------------------
+# GPU leg
+# --------------------------------------------------------------------------------------
+def run_ours(args, cfg, rank, local, world):
+    import ctypes as C
+
+    import torch
+
+    from minisod2d_gb300 import build, capi, workload
+
+    build.build()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    capi.call("msod_init", local)
+    host = workload.HostCase(cfg)
+    dev = workload.DeviceCase(host, device=device)
+    torch.cuda.synchronize()
+    n = cfg.nnode
+    Bc, Bd = algorithmic_bytes(dev.nelem, n, dev.npoin)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        dev.convec()
+        dev.diffu()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        dev.convec()
+        ev[k][1].record(stream)
+        dev.diffu()
+        ev[k][2].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    conv_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in ev]))
+    diff_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in ev]))
+    total_ms = max_over_ranks(total_ms, world, device)
+    ms_step = total_ms / args.steps
+    value = world * 5.0 * dev.npoin / (ms_step * 1e-3) / 1e9
+
+    # e2e through the C ABI with host buffers: H2D of the step's inputs from pinned
+    # memory, both residual calls, D2H of the ten residual arrays.
+    e2e = None
+    if not args.no_e2e:
+        L = capi.lib()
+        ins = {k: getattr(dev, k) for k in ("u", "q", "rho", "pr", "E", "Tem", "mu_fluid", "mu_e", "mu_sgs")}
+        hin = {k: v.cpu().pin_memory() for k, v in ins.items()}
+        outs = [dev.Rmass, dev.Rmom, dev.Rener, dev.Dmass, dev.Dmom, dev.Dener]
+        hout = [torch.empty(o.shape, dtype=o.dtype, pin_memory=True) for o in outs]
+        h2d = sum(v.numel() * v.element_size() for v in hin.values())
+        d2h = sum(o.numel() * o.element_size() for o in outs)
+        st = stream.cuda_stream
+        geo = [cfg.porder, dev.nelem, dev.npoin, dev.connec.data_ptr(), None, None, dev.He.data_ptr(),
+               dev.gpvol.data_ptr(), dev.dlxigp_ip.data_ptr(), None, dev.invAtoIJK.data_ptr(), dev.AtoI.data_ptr(),
+               dev.AtoJ.data_ptr(), dev.AtoK.data_ptr()]
+
+        def e2e_step():
+            for k, v in ins.items():
+                capi.check(L.msod_h2d(v.data_ptr(), hin[k].data_ptr(), v.numel() * v.element_size(), st))
+            capi.check(L.msod_convec_ijk(*geo, dev.u.data_ptr(), dev.q.data_ptr(), dev.rho.data_ptr(),
+                                         dev.pr.data_ptr(), dev.E.data_ptr(), dev.Rmass.data_ptr(),
+                                         dev.Rmom.data_ptr(), dev.Rener.data_ptr(), st))
+            capi.check(L.msod_diffusion_ijk(*geo, C.c_float(cfg.Cp), C.c_float(cfg.Pr), dev.rho.data_ptr(),
+                                            dev.u.data_ptr(), dev.Tem.data_ptr(), dev.mu_fluid.data_ptr(),
+                                            dev.mu_e.data_ptr(), dev.mu_sgs.data_ptr(), dev.Dmass.data_ptr(),
+                                            dev.Dmom.data_ptr(), dev.Dener.data_ptr(), st))
+            for o, h in zip(outs, hout):
+                capi.check(L.msod_d2h(h.data_ptr(), o.data_ptr(), o.numel() * o.element_size(), st))
+
+        for _ in range(args.warmup):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        e2e_ms = max_over_ranks(a.elapsed_time(b), world, device) / args.steps
+        e2e = {"value": world * 5.0 * dev.npoin / (e2e_ms * 1e-3) / 1e9, "unit": "GDOF/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+               "path": "msod_h2d x9 + msod_convec_ijk + msod_diffusion_ijk + msod_d2h x6 (pinned host buffers)"}
+
+    if rank != 0:
+        return
+    peak, peak_kind = peak_hbm()
+    dom = "convec" if conv_ms >= diff_ms else "diffu"
+    dom_ms = conv_ms if dom == "convec" else diff_ms
+    dom_b = Bc if dom == "convec" else Bd
+    achieved = dom_b / (dom_ms * 1e-3) / 1e9
+    tr = load_traffic(cfg.name) or {}
+    traffic = tr.get("convec_ijk" if dom == "convec" else "diffusion_ijk")
+    out = {
+        "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered structured mesh, Fourier fields)",
+        "config": {"workload": cfg.name, "porder": cfg.porder, "nelem": dev.nelem, "npoin": dev.npoin,
+                   "jitter": cfg.jitter, "parallelism": "replica per GPU" if world > 1 else "single GPU",
+                   "l2": "inputs %.2f GB per call > 129 MB L2, no flush" % ((Bc + Bd) / 2e9)},
+        "roofline": {"bound": "hbm", "kernel": dom + " call (output zeroing + kernel)", "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "algorithmic_bytes": dom_b},
+        "kernels": {"convec_ms": conv_ms, "diffu_ms": diff_ms, "convec_gbs": Bc / conv_ms / 1e6,
+                    "diffu_gbs": Bd / diff_ms / 1e6,
+                    "combined_frac": (Bc + Bd) / ((conv_ms + diff_ms) * 1e-3) / 1e9 / peak},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clocks,
+        "e2e": e2e,
+    }
+    if world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(cfg, host, args.cpu_seconds)
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="plain_64")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)  # the timing rules ask for at least 3 warm-up steps
+    from minisod2d_gb300 import workload
+
+    cfg = workload.CONFIGS[args.config]
+    rank, local, world = dist_setup()
+    if args.impl == "reference":
+        if rank == 0:
+            from minisod2d_gb300 import build
+
+            build.build()
+            run_reference(args, cfg)
+        return
+    run_ours(args, cfg, rank, local, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,202 @@
+/*
+ * msod.h -- C ABI of the GB300-native miniSOD2D hex convection/diffusion path.
+ *
+ * Drop-in boundary for the two matrix-free spectral-element kernels of
+ * miniSOD2D (src/kernels/sources/elem_convec.f90, elem_diffu.f90).  Every
+ * entry point is plain C (extern "C", pointers, sizes, no C++ or torch types),
+ * callable from Fortran through ISO_C_BINDING interfaces with scalars passed
+ * by value.
+ *
+ * Conventions shared by all kernel entry points
+ *  - Array arguments are DEVICE pointers (cudaMalloc'd, or msod_malloc'd)
+ *    in the reference's Fortran column-major layouts (E = nelem, n = nnode =
+ *    ngaus = (porder+1)^3, Q = porder+1, 0-based C index formulas):
+ *        connec(nelem,nnode)          connec[a*E+e]            int32, 1-based node ids
+ *        He(3,3,ngaus,nelem)          He[((e*n+g)*3+j)*3+i]    = He(i,j,g,e)
+ *        gpvol(1,ngaus,nelem)         gpvol[e*n+g]
+ *        dlxigp_ip(ngaus,3,Q)         dlxigp_ip[(ii*3+d)*n+g]
+ *        invAtoIJK(Q,Q,Q)             invAtoIJK[(k*Q+j)*Q+i]   int32, 1-based
+ *        gmshAtoI/J/K(nnode)          AtoI[a]                  int32, 1-based
+ *        u,q(npoin,3), Rmom(npoin,3)  u[c*npoin+p]
+ *        mu_e,mu_sgs(nelem,ngaus)     mu_e[g*E+e]
+ *  - Outputs are intent(out): zeroed and then assembled inside the call.
+ *  - Ngp, dNgp and xgp are accepted and ignored, as in the reference, whose
+ *    hex kernels never read them (elem_convec.f90:198-205, elem_diffu.f90:10-16).
+ *    They may be NULL.
+ *  - dlxigp_ip must have the structure hex_highorder gives it
+ *    (elem_hex.f90:23-45): dlxigp_ip(g,d,ii) depends on g only through node
+ *    g's 1-D index in direction d.  The kernels read the 1-D derivative
+ *    matrices from it at every call; msod_check_element_tables verifies the
+ *    structure.
+ *  - `stream` is a cudaStream_t (NULL = the legacy default stream).  Kernel
+ *    calls are asynchronous and stream-ordered; the host returns once the
+ *    work is queued.
+ *  - Return value: MSOD_OK (0) or one of the MSOD_ERR_* codes below.  No
+ *    entry point exits or traps; msod_last_error_string() describes the last
+ *    failure of the calling thread.
+ */
+#ifndef MSOD_H
+#define MSOD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSOD_VERSION 100
+
+#define MSOD_MAX_PORDER 8
+
+#define MSOD_OK 0
+#define MSOD_ERR_INVALID_ARG 1  /* a size, pointer or value outside its contract     */
+#define MSOD_ERR_PORDER 2       /* porder has no compiled instantiation               */
+#define MSOD_ERR_CUDA 3         /* a CUDA runtime call or kernel launch failed        */
+#define MSOD_ERR_BAD_TABLES 4   /* element tables or connectivity failed validation   */
+#define MSOD_ERR_NO_DEVICE 5    /* no usable CUDA device                              */
+#define MSOD_ERR_INTERNAL 6
+#define MSOD_ERR_UNSUPPORTED 7  /* a mode or option this build does not provide       */
+
+/* Field recipes of msod_fields_recipe. */
+#define MSOD_FIELDS_SMOOTH 0 /* rho = 1+0.1 sin sin sin, Fourier u (sigma 0.1), pr = 1+0.05 cos */
+#define MSOD_FIELDS_SHOCK 1  /* tanh density jump + 5% noise, Fourier u (sigma 0.3), Mach 0.8   */
+
+/* ---------------------------------------------------------------------------
+ * Library state and errors
+ * ------------------------------------------------------------------------- */
+
+/* Select the CUDA device used by later calls of this host thread.  Replaces
+ * the reference's implicit OpenACC device initialisation (main.f90:84-94
+ * initialises MPI and the device on first use). */
+int msod_init(int device);
+/* Release library-owned device resources.  Safe to call more than once. */
+int msod_finalize(void);
+/* Text of the last error of the calling thread ("" if none). */
+const char *msod_last_error_string(void);
+int msod_version(void);
+/* Checked mode (default off): every kernel call also validates its element
+ * tables and connectivity on the device and synchronises the stream to report
+ * MSOD_ERR_BAD_TABLES.  Meant for tests and debugging, not timing. */
+int msod_set_checked(int enabled);
+
+/* ---------------------------------------------------------------------------
+ * Device memory (stand-ins for the reference's "!$acc enter data" regions,
+ * main.f90:197-423, for hosts that hold device buffers as type(c_ptr))
+ * ------------------------------------------------------------------------- */
+int msod_malloc(void **ptr, size_t bytes);
+int msod_free(void *ptr);
+int msod_h2d(void *dst_device, const void *src_host, size_t bytes, void *stream);
+int msod_d2h(void *dst_host, const void *src_device, size_t bytes, void *stream);
+int msod_memset(void *dst_device, int value, size_t bytes, void *stream);
+int msod_stream_synchronize(void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Hot path: hex GLL convection and diffusion residuals
+ * ------------------------------------------------------------------------- */
+
+/* full_convec_ijk (elem_convec.f90:198-431).  Rmass, Rmom(npoin,3), Rener
+ * receive the skew-symmetric split-form convection residual.  Rener follows
+ * the complete definition of the split kernel (elem_convec.f90:674-832): the
+ * fused reference kernel reads its energy-flux products without assigning
+ * them (elem_convec.f90:247-250). */
+int msod_convec_ijk(int porder, int nelem, int npoin, const int *connec, const float *Ngp,
+                    const float *dNgp, const float *He, const float *gpvol, const float *dlxigp_ip,
+                    const float *xgp, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
+                    const int *gmshAtoK, const float *u, const float *q, const float *rho,
+                    const float *pr, const float *E, float *Rmass, float *Rmom, float *Rener,
+                    void *stream);
+
+/* full_convec_ijk_split (elem_convec.f90:433-836): same arguments and the same
+ * residuals; served by the same fused single-pass kernel. */
+int msod_convec_ijk_split(int porder, int nelem, int npoin, const int *connec, const float *Ngp,
+                          const float *dNgp, const float *He, const float *gpvol,
+                          const float *dlxigp_ip, const float *xgp, const int *invAtoIJK,
+                          const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK,
+                          const float *u, const float *q, const float *rho, const float *pr,
+                          const float *E, float *Rmass, float *Rmom, float *Rener, void *stream);
+
+/* full_diffusion_ijk (elem_diffu.f90:10-197).  Viscous stress, heat flux and
+ * artificial mass diffusion; nu_e and kappa_e are taken at the output node
+ * (elem_diffu.f90:143-146); c_rho = c_ener = 1 (mod_numerical_params.f90:26-27). */
+int msod_diffusion_ijk(int porder, int nelem, int npoin, const int *connec, const float *Ngp,
+                       const float *dNgp, const float *He, const float *gpvol,
+                       const float *dlxigp_ip, const float *xgp, const int *invAtoIJK,
+                       const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK, float Cp,
+                       float Pr, const float *rho, const float *u, const float *Tem,
+                       const float *mu_fluid, const float *mu_e, const float *mu_sgs, float *Rmass,
+                       float *Rmom, float *Rener, void *stream);
+
+/* FP64 builds of the same kernels (the reference compiled with rp=8,
+ * mod_constants.f90:5): the GPU-side FP64 oracle run. */
+int msod_convec_ijk_f64(int porder, int nelem, int npoin, const int *connec, const double *He,
+                        const double *gpvol, const double *dlxigp_ip, const int *invAtoIJK,
+                        const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK,
+                        const double *u, const double *q, const double *rho, const double *pr,
+                        const double *E, double *Rmass, double *Rmom, double *Rener, void *stream);
+int msod_diffusion_ijk_f64(int porder, int nelem, int npoin, const int *connec, const double *He,
+                           const double *gpvol, const double *dlxigp_ip, const int *invAtoIJK,
+                           const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK,
+                           double Cp, double Pr, const double *rho, const double *u,
+                           const double *Tem, const double *mu_fluid, const double *mu_e,
+                           const double *mu_sgs, double *Rmass, double *Rmom, double *Rener,
+                           void *stream);
+
+/* Validate element tables and connectivity on the device (synchronous):
+ * invAtoIJK is a permutation of 1..n consistent with gmshAtoI/J/K,
+ * dlxigp_ip has the per-direction 1-D structure, every connec entry lies in
+ * 1..npoin.  Returns MSOD_OK or MSOD_ERR_BAD_TABLES. */
+int msod_check_element_tables(int porder, int nelem, int npoin, const int *connec,
+                              const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI,
+                              const int *gmshAtoJ, const int *gmshAtoK, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Element setup (src/fem): metric on the device, tables and mesh on the host
+ * ------------------------------------------------------------------------- */
+
+/* elem_jacobian (jacobian_oper.f90:7-136) on the device: He = Je^-1 by
+ * cofactors and gpvol = wgp*det(Je), Je = dNgp . coord.  Device pointers;
+ * coord(npoin,3) is coord[d*npoin+p]; dNgp(3,nnode,ngaus) is
+ * dNgp[(g*n+a)*3+d].  Rounding follows the reference: no fused
+ * multiply-adds, sums in the reference's order. */
+int msod_elem_jacobian(int porder, int nelem, int npoin, const int *connec, const float *coord,
+                       const float *dNgp, const float *wgp, float *gpvol, float *He, void *stream);
+int msod_elem_jacobian_f64(int porder, int nelem, int npoin, const int *connec,
+                           const double *coord, const double *dNgp, const double *wgp,
+                           double *gpvol, double *He, void *stream);
+
+/* Host: per-element tables of main.f90:110-255 (invAtoIJK, AtoIJK, gmshAtoI/J/K,
+ * xgp(ngaus,3), wgp, Ngp(ngaus,nnode), dNgp(3,nnode,ngaus),
+ * dlxigp_ip(ngaus,3,porder+1)), all host arrays sized by porder. */
+int msod_fem_element_tables(int porder, int *invAtoIJK, int *AtoIJK, int *AtoI, int *AtoJ,
+                            int *AtoK, float *xgp, float *wgp, float *Ngp, float *dNgp,
+                            float *dlxigp_ip);
+int msod_fem_element_tables_f64(int porder, int *invAtoIJK, int *AtoIJK, int *AtoI, int *AtoJ,
+                                int *AtoK, double *xgp, double *wgp, double *Ngp, double *dNgp,
+                                double *dlxigp_ip);
+
+/* Host: structured nx*ny*nz hex mesh of the unit cube with shared nodes,
+ * lexicographic node and element numbering, GLL-spaced high-order nodes placed
+ * by the trilinear map of the element's corner vertices; interior vertices
+ * jittered by up to +-jitter*h per component (seeded).  connec(nelem,nnode)
+ * host array (1-based); coord(npoin,3) host array or NULL.  npoin =
+ * (nx*porder+1)(ny*porder+1)(nz*porder+1).  Replaces create_mesh
+ * (mod_mesh.f90:11-65) for the scaled workloads. */
+int msod_mesh_structured(int porder, int nx, int ny, int nz, const int *AtoI, const int *AtoJ,
+                         const int *AtoK, double jitter, uint64_t seed, int *connec,
+                         float *coord);
+
+/* Host: seeded node fields (FP32) for recipe `kind` with `nmodes` Fourier
+ * modes per velocity component: rho, u(npoin,3), q = rho u, pr,
+ * E = pr/(gamma-1)/rho + |u|^2/2, Tem = pr/(rho Rgas), mu_fluid = 1.8e-5
+ * (gamma = 1.4, Rgas = 287, as main.f90:52).  Replaces the reference's
+ * initial condition (main.f90:320-361). */
+int msod_fields_recipe(int kind, int nmodes, uint64_t seed, int64_t npoin, const float *coord,
+                       float *rho, float *u, float *q, float *pr, float *E, float *Tem,
+                       float *mu_fluid);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSOD_H */

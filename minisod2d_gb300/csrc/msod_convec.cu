@@ -1,0 +1,371 @@
+// msod_convec.cu -- plain (FP32 / FP64) hex GLL convection residual.
+//
+// Computes what full_convec_ijk computes (elem_convec.f90:198-431; Rener as
+// defined by full_convec_ijk_split, elem_convec.f90:674-832):
+//
+//   Rmass  += gpvol [ 1/2 (div q + rho div u) + 1/2 u.grad rho ]
+//   Rmom_i += gpvol [ 1/4 (div F_i + u_i div q + q_i div u + rho div Fuu_i) + d_i p
+//                     + 1/4 sum_j (u_i u_j d_j rho + q_j d_j u_i + u_j d_j q_i) ]
+//   Rener  += gpvol [ 1/4 (div(rho H u) + H div q + rho H div u + rho div(H u))
+//                     + 1/4 sum_i (q_i d_i H + u_i d_i(rho H) + H u_i d_i rho) ]
+//
+// with F = q (x) u, Fuu = u (x) u, k = |u|^2/2 and H = E + k.  The energy
+// residual uses the sums E+k, rho E + rho k, rho E u + rho k u and E u + k u
+// of the reference's separate E and k terms (elem_convec.f90:810-817): the
+// derivatives are linear, so the sums are differentiated once.
+//
+// Design (one group of NE elements per block):
+//   * the block reads the 1-D derivative matrices and node permutations from
+//     the caller's dlxigp_ip / invAtoIJK / gmshAtoI/J/K into shared memory;
+//   * connec is read coalesced along elements (it is element-fastest), node
+//     fields are gathered into a per-element (I,J,K) lattice in shared memory;
+//   * each thread owns one GLL line (S threads share a line at high order).
+//     Three passes (xi, eta, zeta) load the line's nodal values into
+//     registers once, form every differentiated product on the fly and apply
+//     the 1-D derivative matrix held in registers (sum factorisation).  The
+//     residual is linear in the iso-parametric derivatives, so each pass adds
+//     its direction's contribution -- through the He column of that direction
+//     and the point's own nodal values -- to seven per-point accumulators kept
+//     in shared memory;
+//   * the last pass multiplies by gpvol and scatter-adds with red.global.add.
+#include <cuda_runtime.h>
+
+#include "msod_device.cuh"
+#include "msod_kernels.h"
+
+namespace msod {
+namespace {
+
+template <int Q, typename real>
+__device__ __forceinline__ real pick(const real (&a)[Q], int i)
+{
+    real v = a[0];
+#pragma unroll
+    for (int c = 1; c < Q; ++c) v = (i == c) ? a[c] : v;
+    return v;
+}
+
+// Offset of point r of the line (la, lb) running in direction DIR, in the
+// padded shared-memory lattice of one element; and its unpadded lattice index.
+template <int DIR, int Q, int QP>
+__device__ __forceinline__ int line_off(int la, int lb, int r)
+{
+    return DIR == 0 ? (lb * Q + la) * QP + r : (DIR == 1 ? (lb * Q + r) * QP + la : (r * Q + lb) * QP + la);
+}
+template <int DIR, int Q>
+__device__ __forceinline__ int line_lat(int la, int lb, int r)
+{
+    return DIR == 0 ? (lb * Q + la) * Q + r : (DIR == 1 ? (lb * Q + r) * Q + la : (r * Q + lb) * Q + la);
+}
+
+enum { F_RHO = 0, F_P, F_E, F_U0, F_U1, F_U2, F_Q0, F_Q1, F_Q2, NFIELD };
+enum { A_M = 0, A_MOM0, A_MOM1, A_MOM2, A_E, A_DIVU, A_DIVQ, NACC };
+
+template <typename real, int P, int DIR>
+__device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *__restrict__ sA,
+                                            const real *__restrict__ sD, const int *__restrict__ sNode,
+                                            const int *__restrict__ sPerm, const real *__restrict__ He,
+                                            const real *__restrict__ gpvol, int e0, int nelem, int npoin,
+                                            real *__restrict__ Rmass, real *__restrict__ Rmom,
+                                            real *__restrict__ Rener)
+{
+    using G = LineGeom<real, P>;
+    constexpr int Q = G::Q, QP = G::QP, ES = G::ES, NE = G::NE, S = G::S, R = G::R, TPE = G::TPE, N = G::N;
+    constexpr int NPL = NE * ES;
+    constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
+
+    const int tid = threadIdx.x;
+    if (tid >= NE * TPE) return;
+    const int el = tid / TPE, rem = tid - el * TPE;
+    const int line = S == 1 ? rem : rem / S;
+    const int seg = S == 1 ? 0 : rem - line * S;
+    const int la = line % Q, lb = line / Q;
+    const int e = e0 + el;
+    const int base = el * ES + line_off<DIR, Q, QP>(la, lb, 0);
+
+    // Nodal values along the line.
+    real rho_[Q], p_[Q], H_[Q], rH_[Q], u_[3][Q], q_[3][Q];
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        const int o = base + c * OST;
+        rho_[c] = sF[F_RHO * NPL + o];
+        p_[c] = sF[F_P * NPL + o];
+        const real Ev = sF[F_E * NPL + o];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            u_[i][c] = sF[(F_U0 + i) * NPL + o];
+            q_[i][c] = sF[(F_Q0 + i) * NPL + o];
+        }
+        const real k = (real)0.5 * (u_[0][c] * u_[0][c] + u_[1][c] * u_[1][c] + u_[2][c] * u_[2][c]);
+        H_[c] = Ev + k;
+        rH_[c] = rho_[c] * H_[c];
+    }
+
+    // Per owned point: derivative-matrix row, He column DIR, coefficients.
+    const int r0 = seg * R;
+    real Dm[R][Q], h[R][3], own_rho[R], own_H[R], own_rH[R], own_u[R][3], own_q[R][3], cu[R], cq[R];
+    real acc[R][NACC];
+    int gidx[R];
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+        const int r = r0 + rr;
+        const bool ok = (R * S == Q) || r < Q;
+        const int rc = ok ? r : 0;
+#pragma unroll
+        for (int c = 0; c < Q; ++c) Dm[rr][c] = sD[(DIR * Q + rc) * Q + c];
+        const int a = sPerm[line_lat<DIR, Q>(la, lb, rc)];
+        gidx[rr] = a;
+        const real *hp = He + ((size_t)(e < nelem ? e : 0) * N + a) * 9 + DIR * 3;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) h[rr][i] = ldg(hp + i);
+        own_rho[rr] = pick<Q>(rho_, rc);
+        own_H[rr] = pick<Q>(H_, rc);
+        own_rH[rr] = pick<Q>(rH_, rc);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            own_u[rr][i] = pick<Q>(u_[i], rc);
+            own_q[rr][i] = pick<Q>(q_[i], rc);
+        }
+        cu[rr] = own_u[rr][0] * h[rr][0] + own_u[rr][1] * h[rr][1] + own_u[rr][2] * h[rr][2];
+        cq[rr] = own_q[rr][0] * h[rr][0] + own_q[rr][1] * h[rr][1] + own_q[rr][2] * h[rr][2];
+        if (DIR == 0) {
+#pragma unroll
+            for (int k = 0; k < NACC; ++k) acc[rr][k] = (real)0;
+        } else {
+            const int o = base + rc * OST;
+#pragma unroll
+            for (int k = 0; k < NACC; ++k) acc[rr][k] = sA[k * NPL + o];
+        }
+    }
+
+    real d[R], f[Q];
+    auto deriv = [&](const real(&v)[Q]) {
+#pragma unroll
+        for (int rr = 0; rr < R; ++rr) {
+            real s = (real)0;
+#pragma unroll
+            for (int c = 0; c < Q; ++c) s = fma(Dm[rr][c], v[c], s);
+            d[rr] = s;
+        }
+    };
+    const real h4 = (real)0.25, h2 = (real)0.5;
+
+    // rho: mass 1/2 u.grad rho, momentum 1/4 u_i u.grad rho, energy 1/4 H u.grad rho
+    deriv(rho_);
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+        const real t = cu[rr] * d[rr];
+        acc[rr][A_M] = fma(h2, t, acc[rr][A_M]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) acc[rr][A_MOM0 + i] = fma(h4 * own_u[rr][i], t, acc[rr][A_MOM0 + i]);
+        acc[rr][A_E] = fma(h4 * own_H[rr], t, acc[rr][A_E]);
+    }
+    // p: grad p
+    deriv(p_);
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) acc[rr][A_MOM0 + i] = fma(h[rr][i], d[rr], acc[rr][A_MOM0 + i]);
+    // u_i: div u, 1/4 q.grad u_i ; q_i: div q, 1/4 u.grad q_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        deriv(u_[i]);
+#pragma unroll
+        for (int rr = 0; rr < R; ++rr) {
+            acc[rr][A_DIVU] = fma(h[rr][i], d[rr], acc[rr][A_DIVU]);
+            acc[rr][A_MOM0 + i] = fma(h4 * cq[rr], d[rr], acc[rr][A_MOM0 + i]);
+        }
+        deriv(q_[i]);
+#pragma unroll
+        for (int rr = 0; rr < R; ++rr) {
+            acc[rr][A_DIVQ] = fma(h[rr][i], d[rr], acc[rr][A_DIVQ]);
+            acc[rr][A_MOM0 + i] = fma(h4 * cu[rr], d[rr], acc[rr][A_MOM0 + i]);
+        }
+    }
+    // F_ij = q_i u_j: 1/4 div F_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+#pragma unroll
+            for (int c = 0; c < Q; ++c) f[c] = q_[i][c] * u_[j][c];
+            deriv(f);
+#pragma unroll
+            for (int rr = 0; rr < R; ++rr) acc[rr][A_MOM0 + i] = fma(h4 * h[rr][j], d[rr], acc[rr][A_MOM0 + i]);
+        }
+    // Fuu_ij = u_i u_j (symmetric): 1/4 rho div Fuu_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = i; j < 3; ++j) {
+#pragma unroll
+            for (int c = 0; c < Q; ++c) f[c] = u_[i][c] * u_[j][c];
+            deriv(f);
+#pragma unroll
+            for (int rr = 0; rr < R; ++rr) {
+                const real rd = h4 * own_rho[rr] * d[rr];
+                acc[rr][A_MOM0 + i] = fma(h[rr][j], rd, acc[rr][A_MOM0 + i]);
+                if (i != j) acc[rr][A_MOM0 + j] = fma(h[rr][i], rd, acc[rr][A_MOM0 + j]);
+            }
+        }
+    // H: 1/4 q.grad H ; rho H: 1/4 u.grad(rho H)
+    deriv(H_);
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) acc[rr][A_E] = fma(h4 * cq[rr], d[rr], acc[rr][A_E]);
+    deriv(rH_);
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) acc[rr][A_E] = fma(h4 * cu[rr], d[rr], acc[rr][A_E]);
+    // rho H u_i: 1/4 div(rho H u) ; H u_i: 1/4 rho div(H u)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = rH_[c] * u_[i][c];
+        deriv(f);
+#pragma unroll
+        for (int rr = 0; rr < R; ++rr) acc[rr][A_E] = fma(h4 * h[rr][i], d[rr], acc[rr][A_E]);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = H_[c] * u_[i][c];
+        deriv(f);
+#pragma unroll
+        for (int rr = 0; rr < R; ++rr) acc[rr][A_E] = fma(h4 * own_rho[rr] * h[rr][i], d[rr], acc[rr][A_E]);
+    }
+
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+        const int r = r0 + rr;
+        if (!((R * S == Q) || r < Q)) continue;
+        const int o = base + r * OST;
+        if (DIR < 2) {
+#pragma unroll
+            for (int k = 0; k < NACC; ++k) sA[k * NPL + o] = acc[rr][k];
+        } else {
+            const int node = sNode[o];
+            if (node < 0 || e >= nelem) continue;
+            const real divU = acc[rr][A_DIVU], divQ = acc[rr][A_DIVQ];
+            const real gp = ldg(gpvol + (size_t)e * N + gidx[rr]);
+            const real rm = acc[rr][A_M] + h2 * (divQ + own_rho[rr] * divU);
+            const real re = acc[rr][A_E] + h4 * (own_H[rr] * divQ + own_rH[rr] * divU);
+            red_add(Rmass + node, gp * rm);
+            red_add(Rener + node, gp * re);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const real rmom = acc[rr][A_MOM0 + i] + h4 * (own_u[rr][i] * divQ + own_q[rr][i] * divU);
+                red_add(Rmom + (size_t)i * npoin + node, gp * rmom);
+            }
+        }
+    }
+}
+
+template <typename real, int P>
+__global__ void __launch_bounds__(LineGeom<real, P>::NT)
+    convec_kernel(int nelem, int npoin, const int *__restrict__ connec, const real *__restrict__ He,
+                  const real *__restrict__ gpvol, const real *__restrict__ dlxigp_ip,
+                  const int *__restrict__ invAtoIJK, const int *__restrict__ AtoI,
+                  const int *__restrict__ AtoJ, const int *__restrict__ AtoK, const real *__restrict__ u,
+                  const real *__restrict__ q, const real *__restrict__ rho, const real *__restrict__ pr,
+                  const real *__restrict__ E, real *__restrict__ Rmass, real *__restrict__ Rmom,
+                  real *__restrict__ Rener)
+{
+    using G = LineGeom<real, P>;
+    constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT;
+    constexpr int NPL = NE * ES;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    real *sF = reinterpret_cast<real *>(smem_raw);
+    real *sA = sF + NFIELD * NPL;
+    real *sD = sA + NACC * NPL;
+    int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);
+    int *sPerm = sNode + NPL;
+    int *sLat = sPerm + N;
+
+    const int tid = threadIdx.x;
+    const int e0 = blockIdx.x * NE;
+    load_element_tables<real, P>(invAtoIJK, AtoI, AtoJ, AtoK, dlxigp_ip, sPerm, sLat, sD, tid, NT);
+
+    // Node ids of the group's elements; connec is element-fastest.
+    for (int i = tid; i < NE * N; i += NT) {
+        const int el = i % NE, a = i / NE, e = e0 + el;
+        int node = -1;
+        if (e < nelem) {
+            const int v = ldg(connec + (size_t)a * nelem + e) - 1;
+            node = (v >= 0 && v < npoin) ? v : -1;
+        }
+        sNode[el * ES + sLat[a]] = node;
+    }
+    __syncthreads();
+    // Gather node fields into the lattice.
+    const size_t np = (size_t)npoin;
+    for (int i = tid; i < NE * N; i += NT) {
+        const int el = i / N, l = i - el * N;
+        const int I = l % Q, J = (l / Q) % Q, K = l / (Q * Q);
+        const int o = el * ES + (K * Q + J) * QP + I;
+        const int p = sNode[o];
+        real v[NFIELD];
+        if (p >= 0) {
+            v[F_RHO] = ldg(rho + p);
+            v[F_P] = ldg(pr + p);
+            v[F_E] = ldg(E + p);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                v[F_U0 + c] = ldg(u + c * np + p);
+                v[F_Q0 + c] = ldg(q + c * np + p);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < NFIELD; ++c) v[c] = (real)0;
+        }
+#pragma unroll
+        for (int c = 0; c < NFIELD; ++c) sF[c * NPL + o] = v[c];
+    }
+    __syncthreads();
+    convec_pass<real, P, 0>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+    __syncthreads();
+    convec_pass<real, P, 1>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+    __syncthreads();
+    convec_pass<real, P, 2>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+}
+
+template <typename real, int P>
+constexpr size_t convec_smem()
+{
+    using G = LineGeom<real, P>;
+    return (size_t)(NFIELD + NACC) * G::NE * G::ES * sizeof(real) + 3 * G::Q * G::Q * sizeof(real) +
+           (size_t)(G::NE * G::ES + 2 * G::N) * sizeof(int);
+}
+
+template <typename real, int P>
+cudaError_t launch_convec_p(const ConvecArgs<real> &a, cudaStream_t st)
+{
+    using G = LineGeom<real, P>;
+    constexpr size_t smem = convec_smem<real, P>();
+    static_assert(smem <= 227 * 1024, "shared memory budget");
+    cudaError_t err = cudaFuncSetAttribute(convec_kernel<real, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    const unsigned grid = (unsigned)((a.nelem + G::NE - 1) / G::NE);
+    convec_kernel<real, P><<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.dlxigp_ip,
+                                                      a.invAtoIJK, a.AtoI, a.AtoJ, a.AtoK, a.u, a.q, a.rho,
+                                                      a.pr, a.E, a.Rmass, a.Rmom, a.Rener);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+template <typename real>
+cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, cudaStream_t st)
+{
+    switch (porder) {
+    case 1: return launch_convec_p<real, 1>(a, st);
+    case 2: return launch_convec_p<real, 2>(a, st);
+    case 3: return launch_convec_p<real, 3>(a, st);
+    case 4: return launch_convec_p<real, 4>(a, st);
+    case 5: return launch_convec_p<real, 5>(a, st);
+    case 6: return launch_convec_p<real, 6>(a, st);
+    case 7: return launch_convec_p<real, 7>(a, st);
+    case 8: return launch_convec_p<real, 8>(a, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template cudaError_t launch_convec_plain<float>(int, const ConvecArgs<float> &, cudaStream_t);
+template cudaError_t launch_convec_plain<double>(int, const ConvecArgs<double> &, cudaStream_t);
+
+}  // namespace msod

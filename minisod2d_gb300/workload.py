@@ -1,0 +1,135 @@
+"""Named workloads (mesh + seeded fields) and their device residency.
+
+The five workloads of the project's scope:
+  plain_16      16^3 hexes, porder 4, affine, smooth fields (8 modes)         -- CPU-runnable parity case
+  plain_64      64^3 hexes, porder 4, +-5% jitter, smooth fields (8 modes)    -- the throughput workload
+  mixed_p7      32^3 hexes, porder 7, +-5% jitter, smooth fields (16 modes)
+  learned_48    48^3 hexes, porder 4, affine, shock-like fields (8 modes)
+  combined_96   96^3 hexes, porder 5, +-5% jitter, shock-like fields (8 modes)
+All fields are FP32 with seed 0 unless stated; mu_fluid = 1.8e-5,
+mu_e = mu_sgs = 0, Cp = 1004.5, Pr = 0.71.
+"""
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi, fem
+
+
+@dataclass(frozen=True)
+class Config:
+    name: str
+    porder: int
+    nx: int
+    jitter: float
+    kind: int
+    nmodes: int
+    seed: int = 0
+    Cp: float = 1004.5
+    Pr: float = 0.71
+
+    @property
+    def nelem(self):
+        return self.nx ** 3
+
+    @property
+    def npoin(self):
+        return (self.nx * self.porder + 1) ** 3
+
+    @property
+    def nnode(self):
+        return (self.porder + 1) ** 3
+
+
+CONFIGS = {
+    "plain_16": Config("plain_16", 4, 16, 0.0, capi.MSOD_FIELDS_SMOOTH, 8),
+    "plain_64": Config("plain_64", 4, 64, 0.05, capi.MSOD_FIELDS_SMOOTH, 8),
+    "mixed_p7": Config("mixed_p7", 7, 32, 0.05, capi.MSOD_FIELDS_SMOOTH, 16),
+    "learned_48": Config("learned_48", 4, 48, 0.0, capi.MSOD_FIELDS_SHOCK, 8),
+    "combined_96": Config("combined_96", 5, 96, 0.05, capi.MSOD_FIELDS_SHOCK, 8),
+}
+
+
+def custom(porder, nx, jitter=0.0, kind=capi.MSOD_FIELDS_SMOOTH, nmodes=8, seed=0):
+    return Config("custom_p%d_n%d" % (porder, nx), porder, nx, jitter, kind, nmodes, seed)
+
+
+class HostCase:
+    """Host arrays of a workload: element tables, mesh, node fields (numpy)."""
+
+    def __init__(self, cfg, dtype=np.float32):
+        self.cfg = cfg
+        self.tables = fem.element_tables(cfg.porder, np.float32)
+        self.connec, self.coord, self.nelem, self.npoin = fem.structured_mesh(
+            cfg.porder, cfg.nx, cfg.nx, cfg.nx, self.tables, cfg.jitter, cfg.seed)
+        self.fields = fem.fields_recipe(cfg.kind, cfg.nmodes, cfg.seed, self.npoin, self.coord)
+        n = cfg.nnode
+        self.mu_e = np.zeros(self.nelem * n, np.float32)
+        self.mu_sgs = np.zeros(self.nelem * n, np.float32)
+
+
+class DeviceCase:
+    """A workload resident on the GPU as torch tensors, metric built on the device."""
+
+    def __init__(self, host, device="cuda", dtype=None):
+        import torch
+
+        dtype = dtype or torch.float32
+        self.host = host
+        self.cfg = host.cfg
+        self.dtype = dtype
+        self.nelem, self.npoin = host.nelem, host.npoin
+        t = host.tables
+        dev = torch.device(device)
+
+        def up(a, dt=None):
+            return torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
+
+        self.connec = up(host.connec)
+        self.invAtoIJK = up(t["invAtoIJK"])
+        self.AtoI, self.AtoJ, self.AtoK = up(t["AtoI"]), up(t["AtoJ"]), up(t["AtoK"])
+        if dtype == torch.float64:
+            t64 = fem.element_tables(self.cfg.porder, np.float64)
+            self.dlxigp_ip = up(t64["dlxigp_ip"])
+            dN, w = up(t64["dNgp"]), up(t64["wgp"])
+        else:
+            self.dlxigp_ip = up(t["dlxigp_ip"])
+            dN, w = up(t["dNgp"]), up(t["wgp"])
+        coord = up(host.coord, dtype)
+        n = self.cfg.nnode
+        self.He = torch.empty(9 * self.nelem * n, dtype=dtype, device=dev)
+        self.gpvol = torch.empty(self.nelem * n, dtype=dtype, device=dev)
+        from . import kernels
+
+        kernels.elem_jacobian(self.cfg.porder, self.nelem, self.npoin, self.connec, coord, dN, w, self.gpvol, self.He)
+        del coord
+        f = host.fields
+        for k in ("rho", "u", "q", "pr", "E", "Tem", "mu_fluid"):
+            setattr(self, k, up(f[k], dtype))
+        self.mu_e = up(host.mu_e, dtype)
+        self.mu_sgs = up(host.mu_sgs, dtype)
+        self.Rmass = torch.empty(self.npoin, dtype=dtype, device=dev)
+        self.Rmom = torch.empty(3 * self.npoin, dtype=dtype, device=dev)
+        self.Rener = torch.empty(self.npoin, dtype=dtype, device=dev)
+        self.Dmass = torch.empty_like(self.Rmass)
+        self.Dmom = torch.empty_like(self.Rmom)
+        self.Dener = torch.empty_like(self.Rener)
+
+    def geometry(self):
+        return (self.nelem, self.npoin, self.connec, None, None, self.He, self.gpvol, self.dlxigp_ip, None,
+                self.invAtoIJK, self.AtoI, self.AtoJ, self.AtoK)
+
+    def convec(self, split=False, stream=None):
+        from . import kernels
+
+        kernels.full_convec_ijk(*self.geometry(), self.u, self.q, self.rho, self.pr, self.E, self.Rmass, self.Rmom,
+                                self.Rener, stream=stream, split=split)
+        return self.Rmass, self.Rmom, self.Rener
+
+    def diffu(self, stream=None):
+        from . import kernels
+
+        kernels.full_diffusion_ijk(*self.geometry(), self.cfg.Cp, self.cfg.Pr, self.rho, self.u, self.Tem,
+                                   self.mu_fluid, self.mu_e, self.mu_sgs, self.Dmass, self.Dmom, self.Dener,
+                                   stream=stream)
+        return self.Dmass, self.Dmom, self.Dener

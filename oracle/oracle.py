@@ -1,0 +1,185 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Wraps ``libmsod_oracle.so`` (built from ``msod_oracle.c`` by ``build.py``).
+Arrays are numpy arrays in the reference's column-major layouts flattened to
+1-D (see the header of ``msod_oracle.c``); ``dtype`` selects the FP32 (rp=4)
+or FP64 (rp=8) build.  Only tests, ``__graft_entry__.smoke()`` and the CPU
+legs of ``bench.py`` use this module.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _build.build()
+        _lib = C.CDLL(_build.LIB)
+    return _lib
+
+
+def _sfx(dtype):
+    dtype = np.dtype(dtype)
+    if dtype == np.float32:
+        return "_f32"
+    if dtype == np.float64:
+        return "_f64"
+    raise ValueError("oracle dtype must be float32 or float64")
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _c(a, dtype):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a
+
+
+def gll_weights_and_roots(P, dtype=np.float32):
+    w = np.zeros(P + 1, dtype)
+    r = np.zeros(P + 1, dtype)
+    getattr(lib(), "orc_gll_weights_and_roots" + _sfx(dtype))(C.c_int(P), _p(w), _p(r))
+    return w, r
+
+
+def zelegl(P):
+    et = np.zeros(P + 1)
+    vn = np.zeros(P + 1)
+    lib().orc_zelegl_f64(C.c_int(P), _p(et), _p(vn))
+    return et, vn
+
+
+def eval_lagrange_poly(P, xi, xp, dtype=np.float32, deriv=False):
+    xi = _c(xi, dtype)
+    out = np.zeros(P + 1, dtype)
+    name = "orc_eval_lagrange_poly_deriv" if deriv else "orc_eval_lagrange_poly"
+    f = getattr(lib(), name + _sfx(dtype))
+    f.argtypes = [C.c_int, C.c_void_p, C.c_float if np.dtype(dtype) == np.float32 else C.c_double, C.c_void_p]
+    f(P, _p(xi), xp, _p(out))
+    return out
+
+
+def gen_high_order_hex(P):
+    t = np.zeros(((P + 1) ** 3, 3), np.int32)
+    lib().orc_gen_high_order_hex_f32(C.c_int(P), _p(t))
+    return t
+
+
+def element_maps(P):
+    """invAtoIJK (flat, [(k*Q+j)*Q+i]), AtoIJK, AtoI, AtoJ, AtoK -- 1-based."""
+    Q = P + 1
+    n = Q ** 3
+    inv = np.zeros(n, np.int32)
+    atoijk = np.zeros(n, np.int32)
+    ai, aj, ak = (np.zeros(n, np.int32) for _ in range(3))
+    rc = lib().orc_element_maps_f32(C.c_int(P), _p(inv), _p(atoijk), _p(ai), _p(aj), _p(ak))
+    if rc != 0:
+        raise RuntimeError("orc_element_maps failed")
+    return inv, atoijk, ai, aj, ak
+
+
+def element_tables(P, dtype=np.float32):
+    """All per-element reference tables of main.f90:110-255."""
+    inv, atoijk, ai, aj, ak = element_maps(P)
+    n = (P + 1) ** 3
+    xgp = np.zeros(3 * n, dtype)
+    wgp = np.zeros(n, dtype)
+    s = _sfx(dtype)
+    getattr(lib(), "orc_gll_hex" + s)(C.c_int(P), _p(atoijk), _p(xgp), _p(wgp))
+    Ngp = np.zeros(n * n, dtype)
+    dNgp = np.zeros(3 * n * n, dtype)
+    dlx = np.zeros(3 * n * (P + 1), dtype)
+    getattr(lib(), "orc_element_basis" + s)(C.c_int(P), _p(atoijk), _p(xgp), _p(Ngp), _p(dNgp), _p(dlx))
+    return dict(P=P, n=n, invAtoIJK=inv, AtoIJK=atoijk, AtoI=ai, AtoJ=aj, AtoK=ak,
+                xgp=xgp, wgp=wgp, Ngp=Ngp, dNgp=dNgp, dlxigp_ip=dlx)
+
+
+def elem_jacobian(P, nelem, npoin, connec, coord, dNgp, wgp, dtype=np.float32):
+    n = (P + 1) ** 3
+    gpvol = np.zeros(nelem * n, dtype)
+    He = np.zeros(9 * nelem * n, dtype)
+    getattr(lib(), "orc_elem_jacobian" + _sfx(dtype))(
+        C.c_int(P), C.c_int(nelem), C.c_int(npoin), _p(_c(connec, np.int32)), _p(_c(coord, dtype)),
+        _p(_c(dNgp, dtype)), _p(_c(wgp, dtype)), _p(gpvol), _p(He))
+    return He, gpvol
+
+
+def create_mesh_disconnected(P, nelem, xgp, dtype=np.float32):
+    n = (P + 1) ** 3
+    connec = np.zeros(nelem * n, np.int32)
+    coord = np.zeros(3 * nelem * n, dtype)
+    getattr(lib(), "orc_create_mesh_disconnected" + _sfx(dtype))(
+        C.c_int(P), C.c_int(nelem), _p(_c(xgp, dtype)), _p(connec), _p(coord))
+    return connec, coord
+
+
+def reference_ic(P, nelem, npoin, connec, dtype=np.float32):
+    n = (P + 1) ** 3
+    f = {k: np.zeros(npoin, dtype) for k in ("rho", "pr", "E", "Tem", "mu_fluid")}
+    f["u"] = np.zeros(3 * npoin, dtype)
+    f["q"] = np.zeros(3 * npoin, dtype)
+    f["mu_e"] = np.zeros(nelem * n, dtype)
+    f["mu_sgs"] = np.zeros(nelem * n, dtype)
+    getattr(lib(), "orc_reference_ic" + _sfx(dtype))(
+        C.c_int(P), C.c_int(nelem), C.c_int(npoin), _p(_c(connec, np.int32)), _p(f["u"]), _p(f["q"]),
+        _p(f["rho"]), _p(f["pr"]), _p(f["E"]), _p(f["Tem"]), _p(f["mu_fluid"]), _p(f["mu_e"]), _p(f["mu_sgs"]))
+    return f
+
+
+def _geom_args(P, nelem, npoin, g, dtype):
+    return [C.c_int(P), C.c_int(nelem), C.c_int(npoin), _p(g["connec"]), _p(g["He"]), _p(g["gpvol"]),
+            _p(g["dlxigp_ip"]), _p(g["invAtoIJK"]), _p(g["AtoI"]), _p(g["AtoJ"]), _p(g["AtoK"])]
+
+
+def _prep_geom(g, dtype):
+    out = dict(g)
+    for k in ("connec", "invAtoIJK", "AtoI", "AtoJ", "AtoK"):
+        out[k] = _c(g[k], np.int32)
+    for k in ("He", "gpvol", "dlxigp_ip"):
+        out[k] = _c(g[k], dtype)
+    return out
+
+
+def full_convec_ijk(P, nelem, npoin, geom, u, q, rho, pr, E, dtype=np.float32, split=False, nthreads=1):
+    """Rmass, Rmom (3*npoin, component-major), Rener."""
+    g = _prep_geom(geom, dtype)
+    ins = [_c(x, dtype) for x in (u, q, rho, pr, E)]
+    Rmass = np.zeros(npoin, dtype)
+    Rmom = np.zeros(3 * npoin, dtype)
+    Rener = np.zeros(npoin, dtype)
+    name = "orc_full_convec_ijk_split" if split else "orc_full_convec_ijk"
+    rc = getattr(lib(), name + _sfx(dtype))(*_geom_args(P, nelem, npoin, g, dtype), *[_p(x) for x in ins],
+                                          _p(Rmass), _p(Rmom), _p(Rener), C.c_int(nthreads))
+    if rc != 0:
+        raise RuntimeError(name + " failed")
+    return Rmass, Rmom, Rener
+
+
+def full_diffusion_ijk(P, nelem, npoin, geom, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs,
+                       dtype=np.float32, nthreads=1):
+    g = _prep_geom(geom, dtype)
+    ins = [_c(x, dtype) for x in (rho, u, Tem, mu_fluid, mu_e, mu_sgs)]
+    Rmass = np.zeros(npoin, dtype)
+    Rmom = np.zeros(3 * npoin, dtype)
+    Rener = np.zeros(npoin, dtype)
+    real = C.c_float if np.dtype(dtype) == np.float32 else C.c_double
+    rc = getattr(lib(), "orc_full_diffusion_ijk" + _sfx(dtype))(
+        *_geom_args(P, nelem, npoin, g, dtype), real(Cp), real(Pr), *[_p(x) for x in ins],
+        _p(Rmass), _p(Rmom), _p(Rener), C.c_int(nthreads))
+    if rc != 0:
+        raise RuntimeError("orc_full_diffusion_ijk failed")
+    return Rmass, Rmom, Rener
+
+
+def cpu_count():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1

@@ -1,0 +1,33 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")
+
+
+@pytest.fixture(scope="session")
+def msod_lib():
+    from minisod2d_gb300 import build, capi
+
+    build.build()
+    return capi.lib()
+
+
+@pytest.fixture(scope="session")
+def cuda():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from minisod2d_gb300 import build, capi
+
+    build.build()
+    capi.call("msod_init", 0)
+    return torch.device("cuda:0")
