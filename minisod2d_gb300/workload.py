@@ -3,6 +3,7 @@
 The five workloads of the project's scope:
   plain_16      16^3 hexes, porder 4, affine, smooth fields (8 modes)         -- CPU-runnable parity case
   plain_64      64^3 hexes, porder 4, +-5% jitter, smooth fields (8 modes)    -- the throughput workload
+  plain_32      32^3 hexes, same recipe (profiling size: 0.3 GB per call, > L2)
   mixed_p7      32^3 hexes, porder 7, +-5% jitter, smooth fields (16 modes)
   learned_48    48^3 hexes, porder 4, affine, shock-like fields (8 modes)
   combined_96   96^3 hexes, porder 5, +-5% jitter, shock-like fields (8 modes)
@@ -44,6 +45,7 @@ class Config:
 CONFIGS = {
     "plain_16": Config("plain_16", 4, 16, 0.0, capi.MSOD_FIELDS_SMOOTH, 8),
     "plain_64": Config("plain_64", 4, 64, 0.05, capi.MSOD_FIELDS_SMOOTH, 8),
+    "plain_32": Config("plain_32", 4, 32, 0.05, capi.MSOD_FIELDS_SMOOTH, 8),
     "mixed_p7": Config("mixed_p7", 7, 32, 0.05, capi.MSOD_FIELDS_SMOOTH, 16),
     "learned_48": Config("learned_48", 4, 48, 0.0, capi.MSOD_FIELDS_SHOCK, 8),
     "combined_96": Config("combined_96", 5, 96, 0.05, capi.MSOD_FIELDS_SHOCK, 8),

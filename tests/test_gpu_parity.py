@@ -1,9 +1,16 @@
 """GPU parity of the plain kernels against the CPU oracle, through the C ABI.
 
-Tolerance: relative L2 <= 1e-5 per residual in FP32 (atomic scatter order and
-the kernels' re-associated sums differ from the reference's Fortran order);
-<= 1e-11 for the FP64 builds.  Connectivity and index handling are exact by
-construction (the kernels read the caller's connec / invAtoIJK / gmshAtoI/J/K).
+Criterion, per residual (relative L2 over all nodes):
+  * FP32: err32 = |gpu - oracle_fp32| / |oracle_fp32| <= 1e-5.  Where the FP32
+    oracle's own distance from the FP64 oracle on the same inputs (the FP32
+    floor) exceeds 1e-5 -- nested cancellations make it reach ~1.7e-4 for the
+    diffusion energy residual of the smooth workload -- no FP32 evaluation with
+    another summation order can meet 1e-5, and the criterion becomes
+    err32 <= floor and |gpu - oracle_fp64| <= 1.5 * floor: the GPU result is
+    no further from the exact answer than the reference's own FP32 path.
+  * FP64 builds: <= 1e-11 against the FP64 oracle.
+Connectivity and index handling are exact by construction (the kernels read
+the caller's connec / invAtoIJK / gmshAtoI/J/K).
 """
 import os
 
@@ -43,23 +50,40 @@ def _cpu(x):
     return x.cpu().numpy()
 
 
-def _compare(gpu, ref, tol, label):
+def _compare(gpu, ref, tol, label, ref64=None):
+    """Assert the criterion of the module docstring; ref64 (FP64 oracle on the
+    same inputs) enables the floor-aware branch for FP32 results."""
     errs = []
-    for name, g, r in zip(("mass", "mom", "ener"), gpu, ref):
+    for i, (name, g, r) in enumerate(zip(("mass", "mom", "ener"), gpu, ref)):
         g = _cpu(g) if not isinstance(g, np.ndarray) else g
         if np.linalg.norm(r) == 0.0:
             assert np.abs(g).max() == 0.0, (label, name)
-            errs.append(0.0)
+            errs.append((0.0, 0.0, 0.0))
             continue
         e = refimpl.rel_l2(g, r)
-        errs.append(e)
-        assert e <= tol, (label, name, e)
-    print("PARITY %s rel_l2 mass=%.3e mom=%.3e ener=%.3e" % (label, *errs))
+        if ref64 is None:
+            errs.append((e, float("nan"), float("nan")))
+            assert e <= tol, (label, name, e)
+            continue
+        floor = refimpl.rel_l2(r, ref64[i])
+        e64 = refimpl.rel_l2(g, ref64[i])
+        errs.append((e, floor, e64))
+        if e > tol:
+            assert floor > tol and e <= floor and e64 <= 1.5 * floor, (label, name, e, floor, e64)
+    print("PARITY %s " % label + " ".join("%s: err32=%.2e floor=%.2e err64=%.2e" % (n, *x)
+                                          for n, x in zip(("mass", "mom", "ener"), errs)))
     return errs
+
+
+def _geom64(geom):
+    t64 = O.element_tables(geom["P"], np.float64)
+    return dict(t64, connec=geom["connec"], He=geom["He"].astype(np.float64), gpvol=geom["gpvol"].astype(np.float64))
 
 
 def _oracle_convec(host, geom, dtype=np.float32):
     f = host.fields
+    if dtype == np.float64:
+        geom = _geom64(geom)
     return O.full_convec_ijk(host.cfg.porder, host.nelem, host.npoin, geom, f["u"], f["q"], f["rho"], f["pr"],
                              f["E"], dtype, nthreads=NTH)
 
@@ -67,6 +91,8 @@ def _oracle_convec(host, geom, dtype=np.float32):
 def _oracle_diffu(host, geom, dtype=np.float32):
     f = host.fields
     c = host.cfg
+    if dtype == np.float64:
+        geom = _geom64(geom)
     return O.full_diffusion_ijk(c.porder, host.nelem, host.npoin, geom, c.Cp, c.Pr, f["rho"], f["u"], f["Tem"],
                                 f["mu_fluid"], host.mu_e, host.mu_sgs, dtype, nthreads=NTH)
 
@@ -84,15 +110,15 @@ def test_convec_parity_plain_16(cuda):
     """The CPU-runnable workload: 16^3 hexes, porder 4, affine mesh, smooth fields."""
     host, dev = _case(cuda, 4, 16, jitter=0.0)
     g = dev.convec()
-    r = _oracle_convec(host, _geom_host(dev))
-    _compare(g, r, TOL32, "convec plain_16")
+    geom = _geom_host(dev)
+    _compare(g, _oracle_convec(host, geom), TOL32, "convec plain_16", _oracle_convec(host, geom, np.float64))
 
 
 def test_diffu_parity_plain_16(cuda):
     host, dev = _case(cuda, 4, 16, jitter=0.0)
     g = dev.diffu()
-    r = _oracle_diffu(host, _geom_host(dev))
-    _compare(g, r, TOL32, "diffu plain_16")
+    geom = _geom_host(dev)
+    _compare(g, _oracle_diffu(host, geom), TOL32, "diffu plain_16", _oracle_diffu(host, geom, np.float64))
 
 
 @pytest.mark.parametrize("P", range(1, 9))
@@ -100,8 +126,9 @@ def test_parity_all_porders(cuda, P):
     nx = 3 if P <= 4 else 2
     host, dev = _case(cuda, P, nx, jitter=0.05, kind=P % 2, seed=P, mu=2e-3)
     geom = _geom_host(dev)
-    _compare(dev.convec(), _oracle_convec(host, geom), TOL32, "convec P=%d" % P)
-    _compare(dev.diffu(), _oracle_diffu(host, geom), TOL32, "diffu P=%d" % P)
+    _compare(dev.convec(), _oracle_convec(host, geom), TOL32, "convec P=%d" % P,
+             _oracle_convec(host, geom, np.float64))
+    _compare(dev.diffu(), _oracle_diffu(host, geom), TOL32, "diffu P=%d" % P, _oracle_diffu(host, geom, np.float64))
 
 
 @pytest.mark.parametrize("P", [2, 4, 7])
@@ -136,16 +163,20 @@ def test_reference_driver_case(cuda):
     out = [torch.empty(npn, device=cuda), torch.empty(3 * npn, device=cuda), torch.empty(npn, device=cuda)]
     geo = (ne, npn, d["connec"], None, None, d["He"], d["gpvol"], d["dlxigp_ip"], None, d["invAtoIJK"], d["AtoI"],
            d["AtoJ"], d["AtoK"])
+    g64 = _geom64(geom)
     kernels.full_convec_ijk(*geo, d["u"], d["q"], d["rho"], d["pr"], d["E"], *out)
     r = O.full_convec_ijk(P, ne, npn, geom, f["u"], f["q"], f["rho"], f["pr"], f["E"])
-    _compare(out, r, TOL32, "convec reference-driver case")
+    r64 = O.full_convec_ijk(P, ne, npn, g64, f["u"], f["q"], f["rho"], f["pr"], f["E"], np.float64)
+    _compare(out, r, TOL32, "convec reference-driver case", r64)
     kernels.full_convec_ijk_split(*geo, d["u"], d["q"], d["rho"], d["pr"], d["E"], *out)
     r = O.full_convec_ijk(P, ne, npn, geom, f["u"], f["q"], f["rho"], f["pr"], f["E"], split=True)
-    _compare(out, r, TOL32, "convec_split reference-driver case")
+    _compare(out, r, TOL32, "convec_split reference-driver case", r64)
     kernels.full_diffusion_ijk(*geo, 1.0, 1.0, d["rho"], d["u"], d["Tem"], d["mu_fluid"], d["mu_e"], d["mu_sgs"], *out)
     r = O.full_diffusion_ijk(P, ne, npn, geom, 1.0, 1.0, f["rho"], f["u"], f["Tem"], f["mu_fluid"], f["mu_e"],
                              f["mu_sgs"])
-    _compare(out, r, TOL32, "diffu reference-driver case")
+    r64 = O.full_diffusion_ijk(P, ne, npn, g64, 1.0, 1.0, f["rho"], f["u"], f["Tem"], f["mu_fluid"], f["mu_e"],
+                               f["mu_sgs"], np.float64)
+    _compare(out, r, TOL32, "diffu reference-driver case", r64)
 
 
 def test_determinism_and_split_alias(cuda):
@@ -215,46 +246,72 @@ def test_wrong_device_or_dtype_rejected(cuda):
     del torch
 
 
+def _masked(x, m):
+    return [np.asarray(v)[np.tile(m, len(np.asarray(v)) // len(m))] for v in x]
+
+
 def test_sampled_parity_plain_64(cuda):
-    """The throughput workload (64^3 hexes, porder 4, jittered): a slab of 2048
-    elements from the middle of the mesh against the oracle, and the whole mesh
-    against the FP64 build (size-independent precision check)."""
+    """The throughput workload (64^3 hexes, porder 4, jittered).  A slab of four
+    element layers (16384 elements) from the middle of the mesh is run by the
+    kernels and by the FP32/FP64 oracles and compared on the slab's fully
+    assembled nodes (all of their elements lie in the slab).  The whole mesh is
+    then compared with the library's FP64 build, held to the FP32 floor measured
+    on the slab: a size-independent precision check."""
     import torch
 
     host = workload.HostCase(workload.CONFIGS["plain_64"])
     dev = workload.DeviceCase(host, device=cuda)
-    n = host.cfg.nnode
-    e0, e1 = host.nelem // 2, host.nelem // 2 + 2048
+    n, P, nx = host.cfg.nnode, host.cfg.porder, host.cfg.nx
+    z0, z1 = nx // 2 - 2, nx // 2 + 2
+    e0, e1 = z0 * nx * nx, z1 * nx * nx
+    NX = nx * P + 1
+    K = np.arange(host.npoin) // (NX * NX)
+    inner = (K > z0 * P) & (K < z1 * P)
     con = np.ascontiguousarray(host.connec.reshape(n, host.nelem)[:, e0:e1]).reshape(-1)
     He = _cpu(dev.He).reshape(host.nelem, -1)[e0:e1].reshape(-1)
     gp = _cpu(dev.gpvol).reshape(host.nelem, -1)[e0:e1].reshape(-1)
     geom = dict(host.tables, connec=con, He=He, gpvol=gp)
+    g64 = _geom64(geom)
     d_con, d_He, d_gp = (torch.from_numpy(x).to(cuda) for x in (con, He, gp))
     ne = e1 - e0
     geo = (ne, dev.npoin, d_con, None, None, d_He, d_gp, dev.dlxigp_ip, None, dev.invAtoIJK, dev.AtoI, dev.AtoJ,
            dev.AtoK)
-    kernels.full_convec_ijk(*geo, dev.u, dev.q, dev.rho, dev.pr, dev.E, dev.Rmass, dev.Rmom, dev.Rener)
     f = host.fields
-    r = O.full_convec_ijk(4, ne, dev.npoin, geom, f["u"], f["q"], f["rho"], f["pr"], f["E"], nthreads=NTH)
-    _compare((dev.Rmass, dev.Rmom, dev.Rener), r, TOL32, "convec plain_64 slab")
+    kernels.full_convec_ijk(*geo, dev.u, dev.q, dev.rho, dev.pr, dev.E, dev.Rmass, dev.Rmom, dev.Rener)
+    args = (f["u"], f["q"], f["rho"], f["pr"], f["E"])
+    r = O.full_convec_ijk(P, ne, dev.npoin, geom, *args, nthreads=NTH)
+    r64 = O.full_convec_ijk(P, ne, dev.npoin, g64, *args, np.float64, nthreads=NTH)
+    g = [_cpu(x) for x in (dev.Rmass, dev.Rmom, dev.Rener)]
+    cerr = _compare(_masked(g, inner), _masked(r, inner), TOL32, "convec plain_64 slab", _masked(r64, inner))
     mu = np.zeros(ne * n, np.float32)
     d_mu = torch.from_numpy(mu).to(cuda)
     kernels.full_diffusion_ijk(*geo, 1004.5, 0.71, dev.rho, dev.u, dev.Tem, dev.mu_fluid, d_mu, d_mu, dev.Dmass,
                                dev.Dmom, dev.Dener)
-    r = O.full_diffusion_ijk(4, ne, dev.npoin, geom, 1004.5, 0.71, f["rho"], f["u"], f["Tem"], f["mu_fluid"], mu, mu,
-                             nthreads=NTH)
-    _compare((dev.Dmass, dev.Dmom, dev.Dener), r, TOL32, "diffu plain_64 slab")
+    args = (1004.5, 0.71, f["rho"], f["u"], f["Tem"], f["mu_fluid"], mu, mu)
+    r = O.full_diffusion_ijk(P, ne, dev.npoin, geom, *args, nthreads=NTH)
+    r64 = O.full_diffusion_ijk(P, ne, dev.npoin, g64, *args, np.float64, nthreads=NTH)
+    g = [_cpu(x) for x in (dev.Dmass, dev.Dmom, dev.Dener)]
+    derr = _compare(_masked(g, inner), _masked(r, inner), TOL32, "diffu plain_64 slab", _masked(r64, inner))
     # whole mesh: FP32 kernels against the FP64 kernels on the same (FP32-rounded) inputs
     c32 = [x.clone() for x in dev.convec()]
     d32 = [x.clone() for x in dev.diffu()]
     f64 = {k: getattr(dev, k).double() for k in ("u", "q", "rho", "pr", "E", "Tem", "mu_fluid", "mu_e", "mu_sgs")}
     He64, gp64 = dev.He.double(), dev.gpvol.double()
-    dl64 = torch.from_numpy(fem.element_tables(4, np.float64)["dlxigp_ip"]).to(cuda)
+    dl64 = torch.from_numpy(fem.element_tables(P, np.float64)["dlxigp_ip"]).to(cuda)
     geo64 = (dev.nelem, dev.npoin, dev.connec, None, None, He64, gp64, dl64, None, dev.invAtoIJK, dev.AtoI, dev.AtoJ,
              dev.AtoK)
     out = [torch.empty_like(x, dtype=torch.float64) for x in c32]
     kernels.full_convec_ijk(*geo64, f64["u"], f64["q"], f64["rho"], f64["pr"], f64["E"], *out)
-    _compare(c32, [_cpu(x) for x in out], TOL32, "convec plain_64 fp32 vs fp64")
+    for name, a, b, e in zip(("mass", "mom", "ener"), c32, out, cerr):
+        err = refimpl.rel_l2(_cpu(a), _cpu(b))
+        print("PARITY convec plain_64 whole mesh fp32 vs fp64 %s: %.2e (slab floor %.2e)" % (name, err, e[1]))
+        assert err <= max(TOL32, 1.5 * e[1]), (name, err, e)
     kernels.full_diffusion_ijk(*geo64, 1004.5, 0.71, f64["rho"], f64["u"], f64["Tem"], f64["mu_fluid"], f64["mu_e"],
                                f64["mu_sgs"], *out)
-    _compare(d32, [_cpu(x) for x in out], TOL32, "diffu plain_64 fp32 vs fp64")
+    for name, a, b, e in zip(("mass", "mom", "ener"), d32, out, derr):
+        if name == "mass":
+            assert float(torch.abs(a).max()) == 0.0 and float(torch.abs(b).max()) == 0.0
+            continue
+        err = refimpl.rel_l2(_cpu(a), _cpu(b))
+        print("PARITY diffu plain_64 whole mesh fp32 vs fp64 %s: %.2e (slab floor %.2e)" % (name, err, e[1]))
+        assert err <= max(TOL32, 1.5 * e[1]), (name, err, e)
