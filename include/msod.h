@@ -150,6 +150,24 @@ int msod_check_element_tables(int porder, int nelem, int npoin, const int *conne
                               const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI,
                               const int *gmshAtoJ, const int *gmshAtoK, void *stream);
 
+/* No counterpart in the reference.  The same validation as
+ * msod_check_element_tables, for callers that cannot let a library allocate
+ * device memory (a Fortran host whose device memory belongs to the OpenACC
+ * runtime's pool, a process under a capped or pre-reserved allocator, code
+ * that finishes all allocations before capturing a CUDA graph): it calls no
+ * cudaMalloc, cudaFree or allocating routine.  Its scratch is one 32-bit
+ * status word in a static device array that stays resident on every GPU that
+ * loads the library.  Limits are those of the kernel calls (porder <=
+ * MSOD_MAX_PORDER, nelem*nnode < 2^31); larger sizes are rejected with
+ * MSOD_ERR_PORDER / MSOD_ERR_INVALID_ARG.  The first call on a device looks up
+ * the word's device address and should come before any stream capture.
+ * Calls share the word: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
+int msod_check_element_tables_noalloc(int porder, int nelem, int npoin, const int *connec,
+                                      const float *dlxigp_ip, const int *invAtoIJK,
+                                      const int *gmshAtoI, const int *gmshAtoJ,
+                                      const int *gmshAtoK, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Element setup (src/fem): metric on the device, tables and mesh on the host
  * ------------------------------------------------------------------------- */

@@ -46,6 +46,7 @@ SIGNATURES = {
     "msod_convec_ijk_f64": _GEOM64 + [_p] * 8 + [_p],
     "msod_diffusion_ijk_f64": _GEOM64 + [_d, _d] + [_p] * 9 + [_p],
     "msod_check_element_tables": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
+    "msod_check_element_tables_noalloc": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
     "msod_elem_jacobian": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
     "msod_elem_jacobian_f64": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
     "msod_fem_element_tables": [_i] + [_p] * 10,

@@ -1,0 +1,62 @@
+"""The allocation-free table validation, through the C ABI (collected last).
+
+msod_check_element_tables_noalloc serves callers that cannot let the library
+cudaMalloc (an OpenACC-owned device pool, a capped allocator, allocations that
+must precede CUDA-graph capture).  Its verdict must equal that of
+msod_check_element_tables on the same inputs, call after call, and further calls
+must not change the device's free memory.
+"""
+import ctypes as C
+
+import pytest
+
+from minisod2d_gb300 import capi, workload
+
+pytestmark = pytest.mark.gpu
+
+
+def _args(dev, dlx, connec):
+    P = dev.cfg.porder
+    return [P, dev.nelem, dev.npoin, C.c_void_p(connec.data_ptr()), C.c_void_p(dlx.data_ptr()),
+            C.c_void_p(dev.invAtoIJK.data_ptr()), C.c_void_p(dev.AtoI.data_ptr()), C.c_void_p(dev.AtoJ.data_ptr()),
+            C.c_void_p(dev.AtoK.data_ptr()), None]
+
+
+def test_noalloc_validation_matches_allocating_entry_point(cuda):
+    import torch
+
+    L = capi.lib()
+    host = workload.HostCase(workload.Config("noalloc", 4, 2, 0.05, capi.MSOD_FIELDS_SMOOTH, 8, 0))
+    dev = workload.DeviceCase(host, device=cuda)
+    bad_dlx = dev.dlxigp_ip.clone()
+    bad_dlx[7] += 1.0
+    bad_con = dev.connec.clone()
+    bad_con[3] = dev.npoin + 5
+    cases = [("bad tables", _args(dev, bad_dlx, dev.connec)), ("good tables", _args(dev, dev.dlxigp_ip, dev.connec)),
+             ("bad connec", _args(dev, dev.dlxigp_ip, bad_con)), ("good again", _args(dev, dev.dlxigp_ip, dev.connec))]
+    torch.cuda.synchronize()
+    codes = []
+    for label, a in cases:  # consecutive calls: each must start from a cleared status word
+        rc_ref = L.msod_check_element_tables(*a)
+        msg_ref = L.msod_last_error_string()
+        rc_new = L.msod_check_element_tables_noalloc(*a)
+        msg_new = L.msod_last_error_string()
+        assert rc_new == rc_ref, label
+        assert msg_new == msg_ref, label
+        codes.append(rc_new)
+    assert codes == [capi.MSOD_ERR_BAD_TABLES, capi.MSOD_OK, capi.MSOD_ERR_BAD_TABLES, capi.MSOD_OK]
+    # no allocation: the device's free memory is unchanged by further calls
+    good = cases[1][1]
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        assert L.msod_check_element_tables_noalloc(*good) == capi.MSOD_OK
+    assert torch.cuda.mem_get_info()[0] == free0
+    # sizes beyond the limits are rejected before any device work
+    a = list(good)
+    a[0] = capi.MSOD_MAX_PORDER + 1
+    assert L.msod_check_element_tables_noalloc(*a) == capi.MSOD_ERR_PORDER
+    a = list(good)
+    a[1] = 1 << 30
+    assert L.msod_check_element_tables_noalloc(*a) == capi.MSOD_ERR_INVALID_ARG
+    assert b"int32" in L.msod_last_error_string()
