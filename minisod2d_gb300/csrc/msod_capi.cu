@@ -24,9 +24,24 @@ namespace {
 thread_local char g_err[512] = "";
 std::atomic<int> g_checked{0};
 
-// Per-device 4-byte flag word for msod_check_element_tables.
+// Per-device library-owned device memory: the 4-byte flag word of
+// msod_check_element_tables and the per-call element tables of the kernels.
 std::mutex g_mu;
 int *g_flags[64] = {nullptr};
+TableScratch *g_tables[64] = {nullptr};
+
+TableScratch *device_tables()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_tables[dev]) {
+        void *p = nullptr;
+        if (cudaMalloc(&p, sizeof(TableScratch)) != cudaSuccess) return nullptr;
+        g_tables[dev] = static_cast<TableScratch *>(p);
+    }
+    return g_tables[dev];
+}
 
 int *device_flags()
 {
@@ -125,13 +140,14 @@ static int convec_impl(int porder, int nelem, int npoin, const int *connec, cons
         rc = run_check(porder, nelem, npoin, connec, (const float *)dlx, inv, ai, aj, ak, st);
         if (rc) return rc;
     }
+    TableScratch *tabs = nullptr;  // the convection kernel reads the caller's tables itself
     rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
     if (rc) return rc;
     ConvecArgs<real> a;
     a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlx;
     a.invAtoIJK = inv; a.AtoI = ai; a.AtoJ = aj; a.AtoK = ak;
     a.u = u; a.q = q; a.rho = rho; a.pr = pr; a.E = E; a.Rmass = Rmass; a.Rmom = Rmom; a.Rener = Rener;
-    rc = cuda_status(launch_convec_plain<real>(porder, a, st), "convection kernel launch");
+    rc = cuda_status(launch_convec_plain<real>(porder, a, tabs, st), "convection kernel launch");
     if (!rc && checked_mode()) rc = cuda_status(cudaStreamSynchronize(st), "convection kernel");
     return rc;
 }
@@ -153,6 +169,8 @@ static int diffu_impl(int porder, int nelem, int npoin, const int *connec, const
         rc = run_check(porder, nelem, npoin, connec, (const float *)dlx, inv, ai, aj, ak, st);
         if (rc) return rc;
     }
+    TableScratch *tabs = device_tables();
+    if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
     rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
     if (rc) return rc;
     DiffuArgs<real> a;
@@ -160,7 +178,8 @@ static int diffu_impl(int porder, int nelem, int npoin, const int *connec, const
     a.invAtoIJK = inv; a.AtoI = ai; a.AtoJ = aj; a.AtoK = ak; a.Cp = Cp; a.Pr = Pr;
     a.rho = rho; a.u = u; a.Tem = Tem; a.mu_fluid = mu_fluid; a.mu_e = mu_e; a.mu_sgs = mu_sgs;
     a.Rmass = Rmass; a.Rmom = Rmom; a.Rener = Rener;
-    rc = cuda_status(launch_diffu_plain<real>(porder, a, st), "diffusion kernel launch");
+    rc = cuda_status(launch_table_prep<real>(porder, a, tabs, st), "table preparation launch");
+    if (!rc) rc = cuda_status(launch_diffu_plain<real>(porder, a, tabs, st), "diffusion kernel launch");
     if (!rc && checked_mode()) rc = cuda_status(cudaStreamSynchronize(st), "diffusion kernel");
     return rc;
 }
@@ -198,10 +217,12 @@ int msod_finalize(void)
     int cur = 0;
     cudaGetDevice(&cur);
     for (int d = 0; d < 64; ++d)
-        if (g_flags[d]) {
+        if (g_flags[d] || g_tables[d]) {
             cudaSetDevice(d);
-            cudaFree(g_flags[d]);
+            if (g_flags[d]) cudaFree(g_flags[d]);
+            if (g_tables[d]) cudaFree(g_tables[d]);
             g_flags[d] = nullptr;
+            g_tables[d] = nullptr;
         }
     cudaSetDevice(cur);
     return MSOD_OK;

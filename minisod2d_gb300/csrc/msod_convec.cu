@@ -14,7 +14,10 @@
 // of the reference's separate E and k terms (elem_convec.f90:810-817): the
 // derivatives are linear, so the sums are differentiated once.
 //
-// Design (one group of NE elements per block):
+// Design (one group of NE elements per block; this one-shot form measured
+// faster than a persistent, cp.async double-buffered variant of the same
+// passes: the kernel is bound by FP32 issue and He-load latency, not by the
+// gathers):
 //   * the block reads the 1-D derivative matrices and node permutations from
 //     the caller's dlxigp_ip / invAtoIJK / gmshAtoI/J/K into shared memory;
 //   * connec is read coalesced along elements (it is element-fastest), node
@@ -36,6 +39,45 @@
 namespace msod {
 namespace {
 
+// Per-call element tables in shared memory, read from the caller's
+// reference-layout arrays:
+//   perm[l]   lattice point l = (K*Q+J)*Q+I (SOD 1-D indices, 0-based) -> gmsh
+//             local node a (invAtoIJK - 1)
+//   lat[a]    gmsh local node a -> padded lattice offset (K*Q+J)*QP+I
+//             (from gmshAtoI/J/K)
+//   D[d][r][c] = dlxigp_ip(g, d, c) for a point g whose 1-D index in
+//             direction d is r: the 1-D derivative matrix the reference
+//             replicates per point (elem_hex.f90:43-44).
+// Indices are clamped into range, so malformed tables give wrong numbers
+// (caught by msod_check_element_tables), never out-of-bounds accesses.
+template <typename real, int P>
+__device__ __forceinline__ void load_element_tables(const int *__restrict__ invAtoIJK,
+                                                    const int *__restrict__ AtoI,
+                                                    const int *__restrict__ AtoJ,
+                                                    const int *__restrict__ AtoK,
+                                                    const real *__restrict__ dlxigp_ip, int *perm,
+                                                    int *lat, real *D, int tid, int nthreads)
+{
+    using G = LineGeom<real, P>;
+    constexpr int Q = G::Q, N = G::N;
+    for (int i = tid; i < N; i += nthreads) {
+        int a = ldg(invAtoIJK + i) - 1;
+        perm[i] = min(max(a, 0), N - 1);
+        int I = min(max(ldg(AtoI + i) - 1, 0), Q - 1);
+        int J = min(max(ldg(AtoJ + i) - 1, 0), Q - 1);
+        int K = min(max(ldg(AtoK + i) - 1, 0), Q - 1);
+        lat[i] = (K * Q + J) * G::QP + I;
+    }
+    __syncthreads();
+    for (int i = tid; i < 3 * Q * Q; i += nthreads) {
+        const int d = i / (Q * Q), r = (i / Q) % Q, c = i % Q;
+        const int l = d == 0 ? r : (d == 1 ? r * Q : r * Q * Q);
+        const int g = perm[l];
+        D[i] = ldg(dlxigp_ip + (size_t)(c * 3 + d) * N + g);
+    }
+}
+
+
 template <int Q, typename real>
 __device__ __forceinline__ real pick(const real (&a)[Q], int i)
 {
@@ -43,19 +85,6 @@ __device__ __forceinline__ real pick(const real (&a)[Q], int i)
 #pragma unroll
     for (int c = 1; c < Q; ++c) v = (i == c) ? a[c] : v;
     return v;
-}
-
-// Offset of point r of the line (la, lb) running in direction DIR, in the
-// padded shared-memory lattice of one element; and its unpadded lattice index.
-template <int DIR, int Q, int QP>
-__device__ __forceinline__ int line_off(int la, int lb, int r)
-{
-    return DIR == 0 ? (lb * Q + la) * QP + r : (DIR == 1 ? (lb * Q + r) * QP + la : (r * Q + lb) * QP + la);
-}
-template <int DIR, int Q>
-__device__ __forceinline__ int line_lat(int la, int lb, int r)
-{
-    return DIR == 0 ? (lb * Q + la) * Q + r : (DIR == 1 ? (lb * Q + r) * Q + la : (r * Q + lb) * Q + la);
 }
 
 enum { F_RHO = 0, F_P, F_E, F_U0, F_U1, F_U2, F_Q0, F_Q1, F_Q2, NFIELD };
@@ -350,7 +379,7 @@ cudaError_t launch_convec_p(const ConvecArgs<real> &a, cudaStream_t st)
 }  // namespace
 
 template <typename real>
-cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, cudaStream_t st)
+cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, const TableScratch *, cudaStream_t st)
 {
     switch (porder) {
     case 1: return launch_convec_p<real, 1>(a, st);
@@ -365,7 +394,7 @@ cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, cudaStrea
     }
 }
 
-template cudaError_t launch_convec_plain<float>(int, const ConvecArgs<float> &, cudaStream_t);
-template cudaError_t launch_convec_plain<double>(int, const ConvecArgs<double> &, cudaStream_t);
+template cudaError_t launch_convec_plain<float>(int, const ConvecArgs<float> &, const TableScratch *, cudaStream_t);
+template cudaError_t launch_convec_plain<double>(int, const ConvecArgs<double> &, const TableScratch *, cudaStream_t);
 
 }  // namespace msod

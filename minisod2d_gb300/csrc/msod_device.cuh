@@ -32,9 +32,11 @@ __device__ __forceinline__ T ldg(const T *p)
 //   QP = padded row pitch in shared memory (odd, so that line loads along x
 //        hit distinct banks), ES = shared-memory words per element plane.
 //   S  = threads per line (each owns R consecutive points of the line),
-//   NE = elements per block, NT = threads per block.
-template <typename real, int P>
+//   NE = elements per block (at most NECAP), NT = threads per block.
+template <typename real_t, int P_, int NECAP = 64>
 struct LineGeom {
+    using real = real_t;
+    static constexpr int P = P_;
     static constexpr int Q = P + 1;
     static constexpr int L = Q * Q;
     static constexpr int N = Q * Q * Q;
@@ -45,46 +47,77 @@ struct LineGeom {
     static constexpr int TPE = L * S;  // threads per element
     static constexpr int CAP = sizeof(real) == 8 ? (TPE <= 128 ? 128 : ((TPE + 31) / 32) * 32)
                                                  : (TPE <= 32 ? 128 : 256);
-    static constexpr int NE = CAP / TPE > 0 ? CAP / TPE : 1;
+    static constexpr int NE0 = CAP / TPE > 0 ? CAP / TPE : 1;
+    static constexpr int NE = NE0 < NECAP ? NE0 : (NECAP > 0 ? NECAP : 1);
     static constexpr int NT = ((NE * TPE + 31) / 32) * 32;
+    static constexpr int NPL = NE * ES;  // words per shared-memory plane
+    // Blocks per SM the register budget is sized for (__launch_bounds__):
+    // three 128-thread blocks (170 registers) for FP32 up to porder 4.
+    static constexpr int MINB = (sizeof(real) == 4 && NT <= 128) ? 3 : 1;
 };
 
-// Per-call element tables in shared memory, read from the caller's
-// reference-layout arrays:
-//   perm[l]   lattice point l = (K*Q+J)*Q+I (SOD 1-D indices, 0-based) -> gmsh
-//             local node a (invAtoIJK - 1)
-//   lat[a]    gmsh local node a -> padded lattice offset (K*Q+J)*QP+I
-//             (from gmshAtoI/J/K)
-//   D[d][r][c] = dlxigp_ip(g, d, c) for a point g whose 1-D index in
-//             direction d is r: the 1-D derivative matrix the reference
-//             replicates per point (elem_hex.f90:43-44).
-// Indices are clamped into range, so malformed tables give wrong numbers
-// (caught by msod_check_element_tables), never out-of-bounds accesses.
-template <typename real, int P>
-__device__ __forceinline__ void load_element_tables(const int *__restrict__ invAtoIJK,
-                                                    const int *__restrict__ AtoI,
-                                                    const int *__restrict__ AtoJ,
-                                                    const int *__restrict__ AtoK,
-                                                    const real *__restrict__ dlxigp_ip, int *perm,
-                                                    int *lat, real *D, int tid, int nthreads)
+// Largest element count per block whose `planes` shared-memory planes of
+// `bytes` bytes per word fit in `budget` bytes.
+constexpr int necap_for(int planes, int es, int bytes, int budget) { return budget / (planes * es * bytes); }
+
+// Thread -> (element, line, segment) of the line-parallel passes.
+template <class G>
+struct LineThread {
+    int el, la, lb, r0;
+    bool active;
+    __device__ __forceinline__ LineThread(int tid)
+    {
+        active = tid < G::NE * G::TPE;
+        const int t = active ? tid : 0;
+        el = t / G::TPE;
+        const int rem = t - el * G::TPE;
+        const int line = G::S == 1 ? rem : rem / G::S;
+        const int seg = G::S == 1 ? 0 : rem - line * G::S;
+        la = line % G::Q;
+        lb = line / G::Q;
+        r0 = seg * G::R;
+    }
+    __device__ __forceinline__ bool owns(int rr) const { return (G::R * G::S == G::Q) || r0 + rr < G::Q; }
+    __device__ __forceinline__ int rc(int rr) const { return owns(rr) ? r0 + rr : 0; }
+};
+
+// Offset of point r of the line (la, lb) running in direction DIR, in the
+// padded lattice of one element, and its unpadded lattice index.
+template <int DIR, int Q, int QP>
+__device__ __forceinline__ int line_off(int la, int lb, int r)
 {
-    using G = LineGeom<real, P>;
-    constexpr int Q = G::Q, N = G::N;
-    for (int i = tid; i < N; i += nthreads) {
-        int a = ldg(invAtoIJK + i) - 1;
-        perm[i] = min(max(a, 0), N - 1);
-        int I = min(max(ldg(AtoI + i) - 1, 0), Q - 1);
-        int J = min(max(ldg(AtoJ + i) - 1, 0), Q - 1);
-        int K = min(max(ldg(AtoK + i) - 1, 0), Q - 1);
-        lat[i] = (K * Q + J) * G::QP + I;
-    }
-    __syncthreads();
-    for (int i = tid; i < 3 * Q * Q; i += nthreads) {
-        const int d = i / (Q * Q), r = (i / Q) % Q, c = i % Q;
-        const int l = d == 0 ? r : (d == 1 ? r * Q : r * Q * Q);
-        const int g = perm[l];
-        D[i] = ldg(dlxigp_ip + (size_t)(c * 3 + d) * N + g);
-    }
+    return DIR == 0 ? (lb * Q + la) * QP + r : (DIR == 1 ? (lb * Q + r) * QP + la : (r * Q + lb) * QP + la);
+}
+template <int DIR, int Q>
+__device__ __forceinline__ int line_lat(int la, int lb, int r)
+{
+    return DIR == 0 ? (lb * Q + la) * Q + r : (DIR == 1 ? (lb * Q + r) * Q + la : (r * Q + lb) * Q + la);
+}
+
+// Asynchronous 4/8-byte global->shared copies (cp.async); an invalid element is
+// zero-filled without reading global memory.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *dst_smem, const T *src, bool valid)
+{
+    const unsigned saddr = (unsigned)__cvta_generic_to_shared(dst_smem);
+    const int nbytes = valid ? (int)sizeof(T) : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(saddr), "l"(src), "n"(sizeof(T)), "r"(nbytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Grid of a persistent kernel: resident blocks per SM x SMs, capped by the work.
+template <typename Kernel>
+inline int persistent_grid(Kernel kern, int threads, size_t smem, int ngroups)
+{
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, smem) != cudaSuccess) return 0;
+    if (per < 1) per = 1;
+    const long long g = (long long)sms * per;
+    return (int)(g < ngroups ? g : ngroups);
 }
 
 }  // namespace msod

@@ -12,17 +12,21 @@
 //   kappa_e(a) = mu_fluid Cp/Pr + mu_e Cp/Pr + Cp rho mu_sgs / 0.9 evaluated at
 //   the output node (elem_diffu.f90:143-146).
 //
-// Design (one group of NE elements per block, one thread per GLL line):
-//   1. gather rho, T, u, mu_fluid (nodes) and mu_e, mu_sgs (element layout)
-//      into a shared-memory lattice;
-//   2. three line passes store the 15 iso-parametric derivatives per point;
-//   3. a point pass turns them into physical gradients and stress and stores,
+// Design (persistent blocks, groups of NE elements, one thread per GLL line):
+//   0. node ids of group g+2 are loaded into registers and the node fields
+//      (rho, T, u, mu_fluid) plus the element-layout mu_e, mu_sgs of group g+1
+//      are gathered with cp.async into the other half of a double-buffered
+//      shared-memory lattice while group g is computed; the He and gpvol
+//      values of the point pass are loaded into registers before pass 1;
+//   1. three line passes store the 15 iso-parametric derivatives per point;
+//   2. a point pass turns them into physical gradients and stress and stores,
 //      per direction d, the contravariant fluxes gpvol * He(:,d)^T X for the
 //      six vectors X = grad rho, tauU, grad T, tau rows 1..3 (18 per point),
 //      plus nu_e and kappa_e per output node;
-//   4. three line passes apply the transposed 1-D derivative matrix along the
+//   3. three line passes apply the transposed 1-D derivative matrix along the
 //      lines (the weak divergence), accumulating five sums per node through
 //      shared memory; the last pass scatter-adds with red.global.add.
+// The 1-D derivative matrices are constant-bank operands.
 #include <cuda_runtime.h>
 
 #include "msod_device.cuh"
@@ -31,42 +35,37 @@
 namespace msod {
 namespace {
 
+__constant__ float c_Df[MSOD_MAX_PORDER + 1][kTableDMax];
+__constant__ double c_Dd[MSOD_MAX_PORDER + 1][kTableDMax];
+
+template <typename real>
+__device__ __forceinline__ real cD(int P, int i);
+template <>
+__device__ __forceinline__ float cD<float>(int P, int i)
+{
+    return c_Df[P][i];
+}
+template <>
+__device__ __forceinline__ double cD<double>(int P, int i)
+{
+    return c_Dd[P][i];
+}
+
 enum { D_RHO = 0, D_T, D_U0, D_U1, D_U2, D_MUF, D_MUE, D_MUS, NDF };  // gathered planes
 enum { X_GRHO = 0, X_TAUU, X_GT, X_TAU0, X_TAU1, X_TAU2, NX };        // flux vectors
-// After the point pass the gathered planes hold: 0 nu_e, 1 kappa_e, 2..6 partial sums.
-enum { P_NUE = 0, P_KAP = 1, P_DR = 2, P_DE = 3, P_DM0 = 4 };
-
-template <int DIR, int Q, int QP>
-__device__ __forceinline__ int line_off(int la, int lb, int r)
-{
-    return DIR == 0 ? (lb * Q + la) * QP + r : (DIR == 1 ? (lb * Q + r) * QP + la : (r * Q + lb) * QP + la);
-}
+// After the point pass a stage's gathered planes hold: 0 nu_e, 1 kappa_e, 2..6 partial sums.
+enum { P_NUE = 0, P_KAP = 1, P_DR = 2 };
 
 // Pass 1, direction DIR: iso-parametric derivatives of rho, T, u0..2 at the
 // thread's points, stored to planes sX[DIR*5 + f].
-template <typename real, int P, int DIR>
-__device__ __forceinline__ void diffu_grad_pass(const real *__restrict__ sF, real *__restrict__ sX,
-                                                const real *__restrict__ sD)
+template <class G, int DIR>
+__device__ __forceinline__ void grad_pass(const LineThread<G> &lt, const typename G::real *__restrict__ sF,
+                                          typename G::real *__restrict__ sX)
 {
-    using G = LineGeom<real, P>;
-    constexpr int Q = G::Q, QP = G::QP, ES = G::ES, NE = G::NE, S = G::S, R = G::R, TPE = G::TPE;
-    constexpr int NPL = NE * ES;
+    using real = typename G::real;
+    constexpr int P = G::P, Q = G::Q, QP = G::QP, R = G::R, NPL = G::NPL;
     constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
-    const int tid = threadIdx.x;
-    if (tid >= NE * TPE) return;
-    const int el = tid / TPE, rem = tid - el * TPE;
-    const int line = S == 1 ? rem : rem / S;
-    const int seg = S == 1 ? 0 : rem - line * S;
-    const int la = line % Q, lb = line / Q;
-    const int base = el * ES + line_off<DIR, Q, QP>(la, lb, 0);
-    const int r0 = seg * R;
-    real Dm[R][Q];
-#pragma unroll
-    for (int rr = 0; rr < R; ++rr) {
-        const int rc = ((R * S == Q) || r0 + rr < Q) ? r0 + rr : 0;
-#pragma unroll
-        for (int c = 0; c < Q; ++c) Dm[rr][c] = sD[(DIR * Q + rc) * Q + c];
-    }
+    const int base = lt.el * G::ES + line_off<DIR, Q, QP>(lt.la, lt.lb, 0);
 #pragma unroll
     for (int f = 0; f < 5; ++f) {
         real v[Q];
@@ -74,44 +73,32 @@ __device__ __forceinline__ void diffu_grad_pass(const real *__restrict__ sF, rea
         for (int c = 0; c < Q; ++c) v[c] = sF[f * NPL + base + c * OST];
 #pragma unroll
         for (int rr = 0; rr < R; ++rr) {
-            const int r = r0 + rr;
-            if (!((R * S == Q) || r < Q)) continue;
+            if (!lt.owns(rr)) continue;
+            const int row = G::S == 1 ? rr : lt.r0 + rr;
             real s = (real)0;
 #pragma unroll
-            for (int c = 0; c < Q; ++c) s = fma(Dm[rr][c], v[c], s);
-            sX[(DIR * 5 + f) * NPL + base + r * OST] = s;
+            for (int c = 0; c < Q; ++c) s = fma(cD<real>(P, (DIR * Q + row) * Q + c), v[c], s);
+            sX[(DIR * 5 + f) * NPL + base + (lt.r0 + rr) * OST] = s;
         }
     }
 }
 
 // Pass 2, direction DIR: weak divergence along the lines with the transposed
-// derivative matrix; partial sums through planes P_DR..P_DM0+2 of sF.
-template <typename real, int P, int DIR>
-__device__ __forceinline__ void diffu_div_pass(real *__restrict__ sF, const real *__restrict__ sX,
-                                               const real *__restrict__ sD, const int *__restrict__ sNode,
-                                               int e0, int nelem, int npoin, real *__restrict__ Rmass,
-                                               real *__restrict__ Rmom, real *__restrict__ Rener)
+// derivative matrix; partial sums through planes P_DR.. of the stage.
+template <class G, int DIR>
+__device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::real *__restrict__ sF,
+                                         const typename G::real *__restrict__ sX, const int *__restrict__ sNode,
+                                         int npoin, typename G::real *__restrict__ Rmass,
+                                         typename G::real *__restrict__ Rmom, typename G::real *__restrict__ Rener)
 {
-    using G = LineGeom<real, P>;
-    constexpr int Q = G::Q, QP = G::QP, ES = G::ES, NE = G::NE, S = G::S, R = G::R, TPE = G::TPE;
-    constexpr int NPL = NE * ES;
+    using real = typename G::real;
+    constexpr int P = G::P, Q = G::Q, QP = G::QP, R = G::R, NPL = G::NPL;
     constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
-    const int tid = threadIdx.x;
-    if (tid >= NE * TPE) return;
-    const int el = tid / TPE, rem = tid - el * TPE;
-    const int line = S == 1 ? rem : rem / S;
-    const int seg = S == 1 ? 0 : rem - line * S;
-    const int la = line % Q, lb = line / Q;
-    const int base = el * ES + line_off<DIR, Q, QP>(la, lb, 0);
-    const int r0 = seg * R;
-    const int e = e0 + el;
-    real Dt[R][Q], acc[R][5], kap[R];
+    const int base = lt.el * G::ES + line_off<DIR, Q, QP>(lt.la, lt.lb, 0);
+    real acc[R][5], kap[R];
 #pragma unroll
     for (int rr = 0; rr < R; ++rr) {
-        const int rc = ((R * S == Q) || r0 + rr < Q) ? r0 + rr : 0;
-#pragma unroll
-        for (int c = 0; c < Q; ++c) Dt[rr][c] = sD[(DIR * Q + c) * Q + rc];
-        const int o = base + rc * OST;
+        const int o = base + lt.rc(rr) * OST;
         kap[rr] = sF[P_KAP * NPL + o];
 #pragma unroll
         for (int k = 0; k < 5; ++k) acc[rr][k] = DIR == 0 ? (real)0 : sF[(P_DR + k) * NPL + o];
@@ -123,9 +110,10 @@ __device__ __forceinline__ void diffu_div_pass(real *__restrict__ sF, const real
         for (int c = 0; c < Q; ++c) v[c] = sX[(DIR * NX + x) * NPL + base + c * OST];
 #pragma unroll
         for (int rr = 0; rr < R; ++rr) {
+            const int col = G::S == 1 ? rr : lt.rc(rr);
             real s = (real)0;
 #pragma unroll
-            for (int c = 0; c < Q; ++c) s = fma(Dt[rr][c], v[c], s);
+            for (int c = 0; c < Q; ++c) s = fma(cD<real>(P, (DIR * Q + c) * Q + col), v[c], s);
             if (x == X_GRHO) acc[rr][0] += s;
             else if (x == X_TAUU) acc[rr][1] += s;
             else if (x == X_GT) acc[rr][1] = fma(kap[rr], s, acc[rr][1]);
@@ -134,15 +122,14 @@ __device__ __forceinline__ void diffu_div_pass(real *__restrict__ sF, const real
     }
 #pragma unroll
     for (int rr = 0; rr < R; ++rr) {
-        const int r = r0 + rr;
-        if (!((R * S == Q) || r < Q)) continue;
-        const int o = base + r * OST;
+        if (!lt.owns(rr)) continue;
+        const int o = base + (lt.r0 + rr) * OST;
         if (DIR < 2) {
 #pragma unroll
             for (int k = 0; k < 5; ++k) sF[(P_DR + k) * NPL + o] = acc[rr][k];
         } else {
             const int node = sNode[o];
-            if (node < 0 || e >= nelem) continue;
+            if ((unsigned)node >= (unsigned)npoin) continue;
             red_add(Rmass + node, sF[P_NUE * NPL + o] * acc[rr][0]);
             red_add(Rener + node, acc[rr][1]);
 #pragma unroll
@@ -151,179 +138,234 @@ __device__ __forceinline__ void diffu_div_pass(real *__restrict__ sF, const real
     }
 }
 
-template <typename real, int P>
-__global__ void __launch_bounds__(LineGeom<real, P>::NT)
-    diffu_kernel(int nelem, int npoin, const int *__restrict__ connec, const real *__restrict__ He,
-                 const real *__restrict__ gpvol, const real *__restrict__ dlxigp_ip,
-                 const int *__restrict__ invAtoIJK, const int *__restrict__ AtoI, const int *__restrict__ AtoJ,
-                 const int *__restrict__ AtoK, real Cp, real Pr, const real *__restrict__ rho,
-                 const real *__restrict__ u, const real *__restrict__ Tem, const real *__restrict__ mu_fluid,
-                 const real *__restrict__ mu_e, const real *__restrict__ mu_sgs, real *__restrict__ Rmass,
-                 real *__restrict__ Rmom, real *__restrict__ Rener)
+template <class G>
+constexpr size_t diffu_smem_bytes()
 {
-    using G = LineGeom<real, P>;
-    constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT;
-    constexpr int NPL = NE * ES;
+    return (size_t)(2 * NDF + 3 * NX) * G::NPL * sizeof(typename G::real) + (size_t)(2 * G::NPL + 2 * G::N) * sizeof(int);
+}
+
+template <typename real, int P>
+using DiffuGeom = LineGeom<real, P, necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES, (int)sizeof(real), 200 * 1024)>;
+
+template <class G>
+__global__ void __launch_bounds__(G::NT)
+    diffu_kernel(int nelem, int npoin, int ngroups, const int *__restrict__ connec,
+                 const typename G::real *__restrict__ He, const typename G::real *__restrict__ gpvol,
+                 const TableScratch *__restrict__ tabs, typename G::real Cp, typename G::real Pr,
+                 const typename G::real *__restrict__ rho, const typename G::real *__restrict__ u,
+                 const typename G::real *__restrict__ Tem, const typename G::real *__restrict__ mu_fluid,
+                 const typename G::real *__restrict__ mu_e, const typename G::real *__restrict__ mu_sgs,
+                 typename G::real *__restrict__ Rmass, typename G::real *__restrict__ Rmom,
+                 typename G::real *__restrict__ Rener)
+{
+    using real = typename G::real;
+    constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT, NPL = G::NPL;
+    constexpr int IPT = (NE * N + NT - 1) / NT;  // items (node ids, points) per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    real *sF = reinterpret_cast<real *>(smem_raw);  // NDF planes (+1 spare)
-    real *sX = sF + (NDF + 1) * NPL;               // 3*NX planes
-    real *sD = sX + 3 * NX * NPL;
-    int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);
-    int *sPerm = sNode + NPL;
+    real *sF = reinterpret_cast<real *>(smem_raw);  // [2][NDF][NPL]
+    real *sX = sF + 2 * NDF * NPL;                   // [3*NX][NPL]
+    int *sNode = reinterpret_cast<int *>(sX + 3 * NX * NPL);  // [2][NPL]
+    int *sPerm = sNode + 2 * NPL;
     int *sLat = sPerm + N;
 
     const int tid = threadIdx.x;
-    const int e0 = blockIdx.x * NE;
-    load_element_tables<real, P>(invAtoIJK, AtoI, AtoJ, AtoK, dlxigp_ip, sPerm, sLat, sD, tid, NT);
-
-    // Node ids and the element-layout viscosities (element-fastest, coalesced).
-    for (int i = tid; i < NE * N; i += NT) {
-        const int el = i % NE, a = i / NE, e = e0 + el;
-        const int o = el * ES + sLat[a];
-        int node = -1;
-        real me = (real)0, ms = (real)0;
-        if (e < nelem) {
-            const int v = ldg(connec + (size_t)a * nelem + e) - 1;
-            node = (v >= 0 && v < npoin) ? v : -1;
-            me = ldg(mu_e + (size_t)a * nelem + e);
-            ms = ldg(mu_sgs + (size_t)a * nelem + e);
-        }
-        sNode[o] = node;
-        sF[D_MUE * NPL + o] = me;
-        sF[D_MUS * NPL + o] = ms;
+    for (int i = tid; i < N; i += NT) {
+        sPerm[i] = tabs->perm[i];
+        sLat[i] = tabs->lat[i];
     }
-    __syncthreads();
-    const size_t np = (size_t)npoin;
-    for (int i = tid; i < NE * N; i += NT) {
-        const int el = i / N, l = i - el * N;
-        const int I = l % Q, J = (l / Q) % Q, K = l / (Q * Q);
-        const int o = el * ES + (K * Q + J) * QP + I;
-        const int p = sNode[o];
-        real v[6] = {(real)1, (real)0, (real)0, (real)0, (real)0, (real)0};
-        if (p >= 0) {
-            v[0] = ldg(rho + p);
-            v[1] = ldg(Tem + p);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) v[2 + c] = ldg(u + c * np + p);
-            v[5] = ldg(mu_fluid + p);
-        }
-#pragma unroll
-        for (int c = 0; c < 6; ++c) sF[c * NPL + o] = v[c];
-    }
-    __syncthreads();
-    diffu_grad_pass<real, P, 0>(sF, sX, sD);
-    diffu_grad_pass<real, P, 1>(sF, sX, sD);
-    diffu_grad_pass<real, P, 2>(sF, sX, sD);
-    __syncthreads();
 
-    // Point pass: physical gradients, stress and contravariant fluxes.
+    auto load_ids = [&](int g, int (&ids)[IPT]) {
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            const int i = tid + k * NT;
+            const int el = i % NE, a = i / NE, e = g * NE + el;
+            ids[k] = (i < NE * N && e < nelem) ? ldg(connec + (size_t)a * nelem + e) : 0;
+        }
+    };
+    auto store_ids = [&](const int (&ids)[IPT], int *dst) {
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            const int i = tid + k * NT;
+            if (i < NE * N) {
+                const int v = ids[k] - 1;
+                dst[(i % NE) * ES + sLat[i / NE]] = (v >= 0 && v < npoin) ? v : -1;
+            }
+        }
+    };
+    // Node fields in lattice order; mu_e / mu_sgs along elements (coalesced).
+    auto gather = [&](int g, const int *ids_s, real *dst) {
+        for (int i = tid; i < NE * N; i += NT) {
+            const int el = i / N, l = i - el * N;
+            const int I = l % Q, J = (l / Q) % Q, K = l / (Q * Q);
+            const int o = el * ES + (K * Q + J) * QP + I;
+            const int p = ids_s[o];
+            const bool ok = (unsigned)p < (unsigned)npoin;
+            const size_t pp = ok ? (size_t)p : 0, np = (size_t)npoin;
+            cp_async_elem(dst + D_RHO * NPL + o, rho + pp, ok);
+            cp_async_elem(dst + D_T * NPL + o, Tem + pp, ok);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) cp_async_elem(dst + (D_U0 + c) * NPL + o, u + c * np + pp, ok);
+            cp_async_elem(dst + D_MUF * NPL + o, mu_fluid + pp, ok);
+        }
+        for (int i = tid; i < NE * N; i += NT) {
+            const int el = i % NE, a = i / NE, e = g * NE + el;
+            const int o = el * ES + sLat[a];
+            const bool ok = e < nelem;
+            const size_t idx = ok ? (size_t)a * nelem + e : 0;
+            cp_async_elem(dst + D_MUE * NPL + o, mu_e + idx, ok);
+            cp_async_elem(dst + D_MUS * NPL + o, mu_sgs + idx, ok);
+        }
+        cp_async_commit();
+    };
+    // He(:,:) and gpvol of the thread's point-pass points (lattice order).
+    auto load_metric = [&](int g, real (&Hm)[IPT][9], real (&gv)[IPT]) {
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            const int i = tid + k * NT;
+            const int el = i / N, l = i - el * N, e = g * NE + el;
+            const bool ok = i < NE * N && e < nelem;
+            const int a = ok ? sPerm[l] : 0;
+            const real *hp = He + (ok ? ((size_t)e * N + a) * 9 : 0);
+#pragma unroll
+            for (int j = 0; j < 9; ++j) Hm[k][j] = ok ? ldg(hp + j) : (real)0;
+            gv[k] = ok ? ldg(gpvol + (size_t)e * N + a) : (real)0;
+        }
+    };
+
+    int g = blockIdx.x;
+    const int stride = gridDim.x;
+    int ids[IPT];
+    load_ids(g, ids);
+    __syncthreads();  // sLat ready
+    store_ids(ids, sNode);
+    __syncthreads();
+    gather(g, sNode, sF);
+    int gn = g + stride;
+    if (gn < ngroups) load_ids(gn, ids);
+
+    const LineThread<G> lt(tid);
     const real twoThirds = (real)2 / (real)3;
-    for (int i = tid; i < NE * N; i += NT) {
-        const int el = i / N, a = i - el * N, e = e0 + el;
-        const int o = el * ES + sLat[a];
-        real gi[3][5];
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-#pragma unroll
-            for (int f = 0; f < 5; ++f) gi[d][f] = sX[(d * 5 + f) * NPL + o];
-        const real r = sF[D_RHO * NPL + o];
-        const real uu[3] = {sF[D_U0 * NPL + o], sF[D_U1 * NPL + o], sF[D_U2 * NPL + o]};
-        const real muf = sF[D_MUF * NPL + o], me = sF[D_MUE * NPL + o], ms = sF[D_MUS * NPL + o];
-        real Hm[3][3];  // Hm[i][j] = He(i,j)
-        real gp = (real)0;
-        if (e < nelem) {
-            const real *hp = He + ((size_t)e * N + a) * 9;
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-#pragma unroll
-                for (int ii = 0; ii < 3; ++ii) Hm[ii][j] = ldg(hp + j * 3 + ii);
-            gp = ldg(gpvol + (size_t)e * N + a);
-        } else {
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-#pragma unroll
-                for (int ii = 0; ii < 3; ++ii) Hm[ii][j] = (real)0;
+    int s = 0;
+    for (; g < ngroups; g = gn, gn += stride, s ^= 1) {
+        real *sFs = sF + s * NDF * NPL;
+        int *sNs = sNode + s * NPL;
+        real Hm[IPT][9], gv[IPT];
+        load_metric(g, Hm, gv);
+        if (gn < ngroups) store_ids(ids, sNode + (s ^ 1) * NPL);
+        cp_async_wait_all();
+        __syncthreads();
+        if (gn < ngroups) {
+            gather(gn, sNode + (s ^ 1) * NPL, sF + (s ^ 1) * NDF * NPL);
+            if (gn + stride < ngroups) load_ids(gn + stride, ids);
         }
-        real gR[3], gT[3], gU[3][3];
-#pragma unroll
-        for (int ii = 0; ii < 3; ++ii) {
-            gR[ii] = Hm[ii][0] * gi[0][D_RHO] + Hm[ii][1] * gi[1][D_RHO] + Hm[ii][2] * gi[2][D_RHO];
-            gT[ii] = Hm[ii][0] * gi[0][D_T] + Hm[ii][1] * gi[1][D_T] + Hm[ii][2] * gi[2][D_T];
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-                gU[ii][j] = Hm[j][0] * gi[0][D_U0 + ii] + Hm[j][1] * gi[1][D_U0 + ii] + Hm[j][2] * gi[2][D_U0 + ii];
+        if (lt.active) {
+            grad_pass<G, 0>(lt, sFs, sX);
+            grad_pass<G, 1>(lt, sFs, sX);
+            grad_pass<G, 2>(lt, sFs, sX);
         }
-        const real mu_fgp = muf + r * ms;
-        const real mu_tot = mu_fgp + me;
-        const real divU = gU[0][0] + gU[1][1] + gU[2][2];
-        real tau[3][3], tauU[3];
+        __syncthreads();
+        // Point pass: physical gradients, stress and contravariant fluxes.
 #pragma unroll
-        for (int ii = 0; ii < 3; ++ii)
+        for (int k = 0; k < IPT; ++k) {
+            const int i = tid + k * NT;
+            if (i >= NE * N) break;
+            const int el = i / N, l = i - el * N;
+            const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
+            real gi[3][5];
 #pragma unroll
-            for (int j = 0; j < 3; ++j) tau[ii][j] = mu_tot * (gU[ii][j] + gU[j][ii]);
+            for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int ii = 0; ii < 3; ++ii) tau[ii][ii] -= mu_fgp * twoThirds * divU;
+                for (int f = 0; f < 5; ++f) gi[d][f] = sX[(d * 5 + f) * NPL + o];
+            const real r = sFs[D_RHO * NPL + o];
+            const real uu[3] = {sFs[D_U0 * NPL + o], sFs[D_U1 * NPL + o], sFs[D_U2 * NPL + o]};
+            const real muf = sFs[D_MUF * NPL + o], me = sFs[D_MUE * NPL + o], ms = sFs[D_MUS * NPL + o];
+            // Hm[k][j*3+ii] = He(ii, j)
+            real gR[3], gT[3], gU[3][3];
 #pragma unroll
-        for (int ii = 0; ii < 3; ++ii) tauU[ii] = tau[ii][0] * uu[0] + tau[ii][1] * uu[1] + tau[ii][2] * uu[2];
-        const real *Xv[NX] = {gR, tauU, gT, tau[0], tau[1], tau[2]};
+            for (int ii = 0; ii < 3; ++ii) {
+                gR[ii] = Hm[k][ii] * gi[0][D_RHO] + Hm[k][3 + ii] * gi[1][D_RHO] + Hm[k][6 + ii] * gi[2][D_RHO];
+                gT[ii] = Hm[k][ii] * gi[0][D_T] + Hm[k][3 + ii] * gi[1][D_T] + Hm[k][6 + ii] * gi[2][D_T];
 #pragma unroll
-        for (int d = 0; d < 3; ++d)
+                for (int j = 0; j < 3; ++j)
+                    gU[ii][j] = Hm[k][j] * gi[0][D_U0 + ii] + Hm[k][3 + j] * gi[1][D_U0 + ii] +
+                                Hm[k][6 + j] * gi[2][D_U0 + ii];
+            }
+            const real mu_fgp = muf + r * ms;
+            const real mu_tot = mu_fgp + me;
+            const real divU = gU[0][0] + gU[1][1] + gU[2][2];
+            real tau[3][3], tauU[3];
 #pragma unroll
-            for (int x = 0; x < NX; ++x)
-                sX[(d * NX + x) * NPL + o] = gp * (Hm[0][d] * Xv[x][0] + Hm[1][d] * Xv[x][1] + Hm[2][d] * Xv[x][2]);
-        sF[P_NUE * NPL + o] = me / r;
-        sF[P_KAP * NPL + o] = muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
+            for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) tau[ii][j] = mu_tot * (gU[ii][j] + gU[j][ii]);
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii) tau[ii][ii] -= mu_fgp * twoThirds * divU;
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii) tauU[ii] = tau[ii][0] * uu[0] + tau[ii][1] * uu[1] + tau[ii][2] * uu[2];
+            const real *Xv[NX] = {gR, tauU, gT, tau[0], tau[1], tau[2]};
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int x = 0; x < NX; ++x)
+                    sX[(d * NX + x) * NPL + o] =
+                        gv[k] * (Hm[k][d * 3] * Xv[x][0] + Hm[k][d * 3 + 1] * Xv[x][1] + Hm[k][d * 3 + 2] * Xv[x][2]);
+            sFs[P_NUE * NPL + o] = me / r;
+            sFs[P_KAP * NPL + o] = muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
+        }
+        __syncthreads();
+        if (lt.active) div_pass<G, 0>(lt, sFs, sX, sNs, npoin, Rmass, Rmom, Rener);
+        __syncthreads();
+        if (lt.active) div_pass<G, 1>(lt, sFs, sX, sNs, npoin, Rmass, Rmom, Rener);
+        __syncthreads();
+        if (lt.active) div_pass<G, 2>(lt, sFs, sX, sNs, npoin, Rmass, Rmom, Rener);
+        __syncthreads();
     }
-    __syncthreads();
-    diffu_div_pass<real, P, 0>(sF, sX, sD, sNode, e0, nelem, npoin, Rmass, Rmom, Rener);
-    __syncthreads();
-    diffu_div_pass<real, P, 1>(sF, sX, sD, sNode, e0, nelem, npoin, Rmass, Rmom, Rener);
-    __syncthreads();
-    diffu_div_pass<real, P, 2>(sF, sX, sD, sNode, e0, nelem, npoin, Rmass, Rmom, Rener);
 }
 
 template <typename real, int P>
-constexpr size_t diffu_smem()
+cudaError_t launch_diffu_p(const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
-    using G = LineGeom<real, P>;
-    return (size_t)(NDF + 1 + 3 * NX) * G::NE * G::ES * sizeof(real) + 3 * G::Q * G::Q * sizeof(real) +
-           (size_t)(G::NE * G::ES + 2 * G::N) * sizeof(int);
-}
-
-template <typename real, int P>
-cudaError_t launch_diffu_p(const DiffuArgs<real> &a, cudaStream_t st)
-{
-    using G = LineGeom<real, P>;
-    constexpr size_t smem = diffu_smem<real, P>();
+    using G = DiffuGeom<real, P>;
+    constexpr size_t smem = diffu_smem_bytes<G>();
     static_assert(smem <= 227 * 1024, "shared memory budget");
-    cudaError_t err = cudaFuncSetAttribute(diffu_kernel<real, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static_assert(G::NE >= 1, "element group");
+    auto kern = diffu_kernel<G>;
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    const unsigned grid = (unsigned)((a.nelem + G::NE - 1) / G::NE);
-    diffu_kernel<real, P><<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.dlxigp_ip,
-                                                     a.invAtoIJK, a.AtoI, a.AtoJ, a.AtoK, a.Cp, a.Pr, a.rho, a.u,
-                                                     a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.Rmass, a.Rmom, a.Rener);
+    if (sizeof(real) == 4)
+        err = cudaMemcpyToSymbolAsync(c_Df, table_D<float>(tabs), sizeof(float) * 3 * G::Q * G::Q,
+                                      sizeof(float) * kTableDMax * P, cudaMemcpyDeviceToDevice, st);
+    else
+        err = cudaMemcpyToSymbolAsync(c_Dd, table_D<double>(tabs), sizeof(double) * 3 * G::Q * G::Q,
+                                      sizeof(double) * kTableDMax * P, cudaMemcpyDeviceToDevice, st);
+    if (err != cudaSuccess) return err;
+    const int ngroups = (a.nelem + G::NE - 1) / G::NE;
+    const int grid = persistent_grid(kern, G::NT, smem, ngroups);
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    kern<<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, ngroups, a.connec, a.He, a.gpvol, tabs, a.Cp, a.Pr, a.rho, a.u,
+                                    a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.Rmass, a.Rmom, a.Rener);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 template <typename real>
-cudaError_t launch_diffu_plain(int porder, const DiffuArgs<real> &a, cudaStream_t st)
+cudaError_t launch_diffu_plain(int porder, const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
     switch (porder) {
-    case 1: return launch_diffu_p<real, 1>(a, st);
-    case 2: return launch_diffu_p<real, 2>(a, st);
-    case 3: return launch_diffu_p<real, 3>(a, st);
-    case 4: return launch_diffu_p<real, 4>(a, st);
-    case 5: return launch_diffu_p<real, 5>(a, st);
-    case 6: return launch_diffu_p<real, 6>(a, st);
-    case 7: return launch_diffu_p<real, 7>(a, st);
-    case 8: return launch_diffu_p<real, 8>(a, st);
+    case 1: return launch_diffu_p<real, 1>(a, tabs, st);
+    case 2: return launch_diffu_p<real, 2>(a, tabs, st);
+    case 3: return launch_diffu_p<real, 3>(a, tabs, st);
+    case 4: return launch_diffu_p<real, 4>(a, tabs, st);
+    case 5: return launch_diffu_p<real, 5>(a, tabs, st);
+    case 6: return launch_diffu_p<real, 6>(a, tabs, st);
+    case 7: return launch_diffu_p<real, 7>(a, tabs, st);
+    case 8: return launch_diffu_p<real, 8>(a, tabs, st);
     default: return cudaErrorInvalidValue;
     }
 }
 
-template cudaError_t launch_diffu_plain<float>(int, const DiffuArgs<float> &, cudaStream_t);
-template cudaError_t launch_diffu_plain<double>(int, const DiffuArgs<double> &, cudaStream_t);
+template cudaError_t launch_diffu_plain<float>(int, const DiffuArgs<float> &, const TableScratch *, cudaStream_t);
+template cudaError_t launch_diffu_plain<double>(int, const DiffuArgs<double> &, const TableScratch *, cudaStream_t);
 
 }  // namespace msod

@@ -3,7 +3,39 @@
 
 #include <cuda_runtime.h>
 
+#include "msod.h"
+
 namespace msod {
+
+// Per-call element tables written by table_prep_kernel (msod_tables.cu) into a
+// library-owned device area: the 1-D derivative matrices D[d][r][c] (FP32 and
+// FP64 copies), lattice -> gmsh node (perm) and gmsh node -> padded lattice
+// offset (lat).
+constexpr int kTableDMax = 3 * (MSOD_MAX_PORDER + 1) * (MSOD_MAX_PORDER + 1);
+constexpr int kTableNMax = (MSOD_MAX_PORDER + 1) * (MSOD_MAX_PORDER + 1) * (MSOD_MAX_PORDER + 1);
+struct TableScratch {
+    float Df[kTableDMax];
+    double Dd[kTableDMax];
+    int perm[kTableNMax];
+    int lat[kTableNMax];
+};
+template <typename real>
+__host__ __device__ inline real *table_D(TableScratch *t);
+template <>
+__host__ __device__ inline float *table_D<float>(TableScratch *t)
+{
+    return t->Df;
+}
+template <>
+__host__ __device__ inline double *table_D<double>(TableScratch *t)
+{
+    return t->Dd;
+}
+template <typename real>
+__host__ __device__ inline const real *table_D(const TableScratch *t)
+{
+    return table_D<real>(const_cast<TableScratch *>(t));
+}
 
 template <typename real>
 struct ElementArgs {
@@ -26,11 +58,15 @@ struct DiffuArgs : ElementArgs<real> {
     real *Rmass, *Rmom, *Rener;
 };
 
-// Plain kernels (outputs must be zeroed by the caller).
+// Tables of one call (one block, stream-ordered before the kernels).
 template <typename real>
-cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, cudaStream_t st);
+cudaError_t launch_table_prep(int porder, const ElementArgs<real> &a, TableScratch *scratch, cudaStream_t st);
+
+// Plain kernels (outputs must be zeroed by the caller; tables prepared).
 template <typename real>
-cudaError_t launch_diffu_plain(int porder, const DiffuArgs<real> &a, cudaStream_t st);
+cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, const TableScratch *tabs, cudaStream_t st);
+template <typename real>
+cudaError_t launch_diffu_plain(int porder, const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st);
 
 // Setup kernels.
 template <typename real>

@@ -1,0 +1,77 @@
+// msod_tables.cu -- per-call element tables for the line-parallel kernels.
+//
+// Every kernel call first runs table_prep_kernel, one block that reads the
+// caller's dlxigp_ip / invAtoIJK / gmshAtoI/J/K (device arrays in the
+// reference's layouts) and writes, into a small library-owned device area:
+//   perm[l]  lattice point l = (K*Q+J)*Q+I (SOD 1-D indices) -> gmsh node a
+//   lat[a]   gmsh node a -> padded shared-memory lattice offset (K*Q+J)*QP+I
+//   D[d][r][c] = dlxigp_ip(g, d, c) for a point g whose 1-D index in
+//            direction d is r: the 1-D derivative matrix the reference
+//            replicates per point (elem_hex.f90:43-44, mod_maths.f90:274-281).
+// The kernels copy D into their constant bank (so the contractions take
+// their coefficients as constant operands) and perm/lat into shared memory.
+// Indices are clamped, so malformed tables give wrong numbers (reported by
+// msod_check_element_tables), never out-of-bounds accesses.
+#include <cuda_runtime.h>
+
+#include "msod_device.cuh"
+#include "msod_kernels.h"
+
+namespace msod {
+namespace {
+
+template <typename real, int P>
+__global__ void table_prep_kernel(const int *__restrict__ invAtoIJK, const int *__restrict__ AtoI,
+                                  const int *__restrict__ AtoJ, const int *__restrict__ AtoK,
+                                  const real *__restrict__ dlxigp_ip, TableScratch *out)
+{
+    using G = LineGeom<real, P>;
+    constexpr int Q = G::Q, N = G::N;
+    __shared__ int sperm[N];
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const int a = min(max(invAtoIJK[i] - 1, 0), N - 1);
+        sperm[i] = a;
+        out->perm[i] = a;
+        const int I = min(max(AtoI[i] - 1, 0), Q - 1);
+        const int J = min(max(AtoJ[i] - 1, 0), Q - 1);
+        const int K = min(max(AtoK[i] - 1, 0), Q - 1);
+        out->lat[i] = (K * Q + J) * G::QP + I;
+    }
+    __syncthreads();
+    real *D = table_D<real>(out);
+    for (int i = threadIdx.x; i < 3 * Q * Q; i += blockDim.x) {
+        const int d = i / (Q * Q), r = (i / Q) % Q, c = i % Q;
+        const int l = d == 0 ? r : (d == 1 ? r * Q : r * Q * Q);
+        D[i] = dlxigp_ip[(size_t)(c * 3 + d) * N + sperm[l]];
+    }
+}
+
+template <typename real, int P>
+cudaError_t prep_p(const ElementArgs<real> &a, TableScratch *scratch, cudaStream_t st)
+{
+    table_prep_kernel<real, P><<<1, 256, 0, st>>>(a.invAtoIJK, a.AtoI, a.AtoJ, a.AtoK, a.dlxigp_ip, scratch);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+template <typename real>
+cudaError_t launch_table_prep(int porder, const ElementArgs<real> &a, TableScratch *scratch, cudaStream_t st)
+{
+    switch (porder) {
+    case 1: return prep_p<real, 1>(a, scratch, st);
+    case 2: return prep_p<real, 2>(a, scratch, st);
+    case 3: return prep_p<real, 3>(a, scratch, st);
+    case 4: return prep_p<real, 4>(a, scratch, st);
+    case 5: return prep_p<real, 5>(a, scratch, st);
+    case 6: return prep_p<real, 6>(a, scratch, st);
+    case 7: return prep_p<real, 7>(a, scratch, st);
+    case 8: return prep_p<real, 8>(a, scratch, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template cudaError_t launch_table_prep<float>(int, const ElementArgs<float> &, TableScratch *, cudaStream_t);
+template cudaError_t launch_table_prep<double>(int, const ElementArgs<double> &, TableScratch *, cudaStream_t);
+
+}  // namespace msod
