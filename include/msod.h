@@ -57,6 +57,11 @@ extern "C" {
 #define MSOD_ERR_NO_DEVICE 5    /* no usable CUDA device                              */
 #define MSOD_ERR_INTERNAL 6
 #define MSOD_ERR_UNSUPPORTED 7  /* a mode or option this build does not provide       */
+#define MSOD_ERR_BAD_MODEL 8    /* a network weight file is malformed or fails its CRC */
+
+/* Per-element learned viscosity: 12 features -> 32 -> 32 -> 1 parameters. */
+#define MSOD_MLP_NFEATURES 12
+#define MSOD_MLP_NPARAMS 1505
 
 /* Field recipes of msod_fields_recipe. */
 #define MSOD_FIELDS_SMOOTH 0 /* rho = 1+0.1 sin sin sin, Fourier u (sigma 0.1), pr = 1+0.05 cos */
@@ -212,6 +217,76 @@ int msod_mesh_structured(int porder, int nx, int ny, int nz, const int *AtoI, co
 int msod_fields_recipe(int kind, int nmodes, uint64_t seed, int64_t npoin, const float *coord,
                        float *rho, float *u, float *q, float *pr, float *E, float *Tem,
                        float *mu_fluid);
+
+/* ---------------------------------------------------------------------------
+ * Artificial viscosity mu_e: plain entropy-viscosity estimator and the
+ * learned per-element estimator.  No counterpart in the reference, which
+ * consumes mu_e(nelem,ngaus) (elem_diffu.f90:19) without computing it; the
+ * knobs follow mod_numerical_params.f90:22-28 (ce = 0.1, cmax = 0.5,
+ * normalised entropy).
+ * ------------------------------------------------------------------------- */
+
+/* Entropy-viscosity estimator (Guermond, Pasquetti & Popov, JCP 230 (2011)):
+ * eta = rho/(gamma-1) log(p/rho^gamma), R = div(eta u) - eta div u - u.grad eta,
+ * per element nu = min(cmax h max(|u|+c), ce h^2 max|R| / ||eta - mean eta||_inf)
+ * with h = (sum gpvol)^(1/3)/porder; mu_e(e,a) = rho(a) nu(e) in the reference's
+ * mu_e(nelem,ngaus) layout.  nu_elem / numax_elem (nelem each) may be NULL.
+ * porder 1..7. */
+int msod_entropy_viscosity(int porder, int nelem, int npoin, const int *connec, const float *He,
+                           const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK,
+                           const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK,
+                           const float *rho, const float *u, const float *pr, float gamma, float ce,
+                           float cmax, int normalise, float *mu_e, float *nu_elem,
+                           float *numax_elem, void *stream);
+
+/* The 12 element features of the learned estimator (feat[e*12+k]) and the
+ * element's first-order viscosity nu_max.  p_or_T is the pressure (Rgas = 0)
+ * or the temperature with p = rho Rgas T. */
+int msod_mlp_features(int porder, int nelem, int npoin, const int *connec, const float *He,
+                      const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK,
+                      const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK,
+                      const float *rho, const float *u, const float *p_or_T, float Rgas, float gamma,
+                      float cmax, float *feat, float *numax_elem, void *stream);
+
+/* Network handle: device weights (FP32 master, FP16 deployed copy), Adam
+ * state and the feature normalisation (mean, 1/std, training min, max). */
+typedef struct msod_mlp msod_mlp;
+int msod_mlp_create(msod_mlp **out, uint64_t seed);
+int msod_mlp_destroy(msod_mlp *m);
+/* Adam on mean-squared error of y = nu/nu_max over nsamples device pairs
+ * (feat[nsamples*12], target[nsamples]); batch samples drawn per step from
+ * `seed`; the feature normalisation is set from the training data.
+ * loss_host (steps floats) may be NULL.  Synchronous. */
+int msod_mlp_train(msod_mlp *m, const float *feat, const float *target, int nsamples, int steps,
+                   int batch, float lr, uint64_t seed, float *loss_host, void *stream);
+/* Batch gradient of the loss at the current weights (for gradient checks). */
+int msod_mlp_gradient(msod_mlp *m, const float *feat, const float *target, const int *idx, int batch,
+                      float *grad_host, void *stream);
+int msod_mlp_get_params(const msod_mlp *m, float *params_host, float *norm_host);
+int msod_mlp_set_params(msod_mlp *m, const float *params_host, const float *norm_host);
+/* y = network output clipped to [0,1], nu = y*numax (if numax given), flag = 1
+ * where a feature lies outside the training range. */
+int msod_mlp_predict(const msod_mlp *m, const float *feat, const float *numax_elem, int nelem, float *y,
+                     float *nu_elem, int *flag, void *stream);
+/* Weight file with a CRC-32; a failed check returns MSOD_ERR_BAD_MODEL. */
+int msod_mlp_save(const msod_mlp *m, const char *path);
+int msod_mlp_load(msod_mlp *m, const char *path);
+/* nu per element from the network; elements flagged out of range take the
+ * plain estimator's value. */
+int msod_learned_viscosity(const msod_mlp *m, int porder, int nelem, int npoin, const int *connec,
+                           const float *He, const float *gpvol, const float *dlxigp_ip,
+                           const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
+                           const int *gmshAtoK, const float *rho, const float *u, const float *p_or_T,
+                           float Rgas, float gamma, float ce, float cmax, float *nu_elem, int *flag,
+                           void *stream);
+/* full_diffusion_ijk with mu_e(e,a) = rho(a) nu_elem(e): one viscosity value
+ * per element instead of the mu_e(nelem,ngaus) array. */
+int msod_diffusion_ijk_nu(int porder, int nelem, int npoin, const int *connec, const float *He,
+                          const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK,
+                          const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK, float Cp,
+                          float Pr, const float *rho, const float *u, const float *Tem,
+                          const float *mu_fluid, const float *nu_elem, const float *mu_sgs,
+                          float *Rmass, float *Rmom, float *Rener, void *stream);
 
 #ifdef __cplusplus
 }

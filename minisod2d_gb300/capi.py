@@ -19,6 +19,7 @@ MSOD_ERR_BAD_TABLES = 4
 MSOD_ERR_NO_DEVICE = 5
 MSOD_ERR_INTERNAL = 6
 MSOD_ERR_UNSUPPORTED = 7
+MSOD_ERR_BAD_MODEL = 8
 MSOD_MAX_PORDER = 8
 MSOD_FIELDS_SMOOTH = 0
 MSOD_FIELDS_SHOCK = 1
@@ -53,6 +54,19 @@ SIGNATURES = {
     "msod_fem_element_tables_f64": [_i] + [_p] * 10,
     "msod_mesh_structured": [_i, _i, _i, _i, _p, _p, _p, _d, _u64, _p, _p],
     "msod_fields_recipe": [_i, _i, _u64, _i64, _p, _p, _p, _p, _p, _p, _p, _p],
+    "msod_entropy_viscosity": [_i, _i, _i] + [_p] * 8 + [_p, _p, _p, _f, _f, _f, _i, _p, _p, _p, _p],
+    "msod_mlp_features": [_i, _i, _i] + [_p] * 8 + [_p, _p, _p, _f, _f, _f, _p, _p, _p],
+    "msod_mlp_create": [C.POINTER(_p), _u64],
+    "msod_mlp_destroy": [_p],
+    "msod_mlp_train": [_p, _p, _p, _i, _i, _i, _f, _u64, _p, _p],
+    "msod_mlp_gradient": [_p, _p, _p, _p, _i, _p, _p],
+    "msod_mlp_get_params": [_p, _p, _p],
+    "msod_mlp_set_params": [_p, _p, _p],
+    "msod_mlp_predict": [_p, _p, _p, _i, _p, _p, _p, _p],
+    "msod_mlp_save": [_p, C.c_char_p],
+    "msod_mlp_load": [_p, C.c_char_p],
+    "msod_learned_viscosity": [_p, _i, _i, _i] + [_p] * 8 + [_p, _p, _p, _f, _f, _f, _f, _p, _p, _p],
+    "msod_diffusion_ijk_nu": [_i, _i, _i] + [_p] * 8 + [_f, _f] + [_p] * 9 + [_p],
 }
 
 

@@ -147,7 +147,7 @@ constexpr size_t diffu_smem_bytes()
 template <typename real, int P>
 using DiffuGeom = LineGeom<real, P, necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES, (int)sizeof(real), 200 * 1024)>;
 
-template <class G>
+template <class G, bool NUE>
 __global__ void __launch_bounds__(G::NT)
     diffu_kernel(int nelem, int npoin, int ngroups, const int *__restrict__ connec,
                  const typename G::real *__restrict__ He, const typename G::real *__restrict__ gpvol,
@@ -155,8 +155,8 @@ __global__ void __launch_bounds__(G::NT)
                  const typename G::real *__restrict__ rho, const typename G::real *__restrict__ u,
                  const typename G::real *__restrict__ Tem, const typename G::real *__restrict__ mu_fluid,
                  const typename G::real *__restrict__ mu_e, const typename G::real *__restrict__ mu_sgs,
-                 typename G::real *__restrict__ Rmass, typename G::real *__restrict__ Rmom,
-                 typename G::real *__restrict__ Rener)
+                 const typename G::real *__restrict__ nu_elem, typename G::real *__restrict__ Rmass,
+                 typename G::real *__restrict__ Rmom, typename G::real *__restrict__ Rener)
 {
     using real = typename G::real;
     constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT, NPL = G::NPL;
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(G::NT)
             const int o = el * ES + sLat[a];
             const bool ok = e < nelem;
             const size_t idx = ok ? (size_t)a * nelem + e : 0;
-            cp_async_elem(dst + D_MUE * NPL + o, mu_e + idx, ok);
+            if (!NUE) cp_async_elem(dst + D_MUE * NPL + o, mu_e + idx, ok);
             cp_async_elem(dst + D_MUS * NPL + o, mu_sgs + idx, ok);
         }
         cp_async_commit();
@@ -278,7 +278,9 @@ __global__ void __launch_bounds__(G::NT)
                 for (int f = 0; f < 5; ++f) gi[d][f] = sX[(d * 5 + f) * NPL + o];
             const real r = sFs[D_RHO * NPL + o];
             const real uu[3] = {sFs[D_U0 * NPL + o], sFs[D_U1 * NPL + o], sFs[D_U2 * NPL + o]};
-            const real muf = sFs[D_MUF * NPL + o], me = sFs[D_MUE * NPL + o], ms = sFs[D_MUS * NPL + o];
+            const int ee = g * NE + el;
+            const real muf = sFs[D_MUF * NPL + o], ms = sFs[D_MUS * NPL + o];
+            const real me = NUE ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0) : sFs[D_MUE * NPL + o];
             // Hm[k][j*3+ii] = He(ii, j)
             real gR[3], gT[3], gU[3][3];
 #pragma unroll
@@ -322,14 +324,14 @@ __global__ void __launch_bounds__(G::NT)
     }
 }
 
-template <typename real, int P>
-cudaError_t launch_diffu_p(const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
+template <typename real, int P, bool NUE>
+cudaError_t launch_diffu_pn(const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
     using G = DiffuGeom<real, P>;
     constexpr size_t smem = diffu_smem_bytes<G>();
     static_assert(smem <= 227 * 1024, "shared memory budget");
     static_assert(G::NE >= 1, "element group");
-    auto kern = diffu_kernel<G>;
+    auto kern = diffu_kernel<G, NUE>;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     if (sizeof(real) == 4)
@@ -343,8 +345,15 @@ cudaError_t launch_diffu_p(const DiffuArgs<real> &a, const TableScratch *tabs, c
     const int grid = persistent_grid(kern, G::NT, smem, ngroups);
     if (grid <= 0) return cudaErrorInvalidConfiguration;
     kern<<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, ngroups, a.connec, a.He, a.gpvol, tabs, a.Cp, a.Pr, a.rho, a.u,
-                                    a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.Rmass, a.Rmom, a.Rener);
+                                    a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.nu_elem, a.Rmass, a.Rmom, a.Rener);
     return cudaGetLastError();
+}
+
+template <typename real, int P>
+cudaError_t launch_diffu_p(const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
+{
+    if (a.nu_elem) return launch_diffu_pn<real, P, true>(a, tabs, st);
+    return launch_diffu_pn<real, P, false>(a, tabs, st);
 }
 
 }  // namespace

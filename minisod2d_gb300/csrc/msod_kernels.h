@@ -1,6 +1,7 @@
 // msod_kernels.h -- launcher interfaces between the C-ABI layer and the kernels.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "msod.h"
@@ -55,6 +56,7 @@ template <typename real>
 struct DiffuArgs : ElementArgs<real> {
     real Cp, Pr;
     const real *rho, *u, *Tem, *mu_fluid, *mu_e, *mu_sgs;
+    const real *nu_elem;  // if set: mu_e(e, a) = rho(a) * nu_elem[e] and mu_e is not read
     real *Rmass, *Rmom, *Rener;
 };
 
@@ -67,6 +69,66 @@ template <typename real>
 cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, const TableScratch *tabs, cudaStream_t st);
 template <typename real>
 cudaError_t launch_diffu_plain(int porder, const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Entropy viscosity and the learned estimator
+// ---------------------------------------------------------------------------
+struct EntropyStats {
+    double sum;  // sum of eta over the nodes
+    int kmin;    // order-preserving int keys of min / max eta
+    int kmax;
+};
+
+constexpr int kMlpIn = 12, kMlpH = 32;
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kMlpH * kMlpIn;
+constexpr int kOffW2 = kOffB1 + kMlpH;
+constexpr int kOffB2 = kOffW2 + kMlpH * kMlpH;
+constexpr int kOffW3 = kOffB2 + kMlpH;
+constexpr int kOffB3 = kOffW3 + kMlpH;
+constexpr int kMlpParams = kOffB3 + 1;  // 1505
+static_assert(kMlpParams == MSOD_MLP_NPARAMS, "parameter count");
+
+struct MlpNorm {
+    float mean[kMlpIn], inv_std[kMlpIn], fmin[kMlpIn], fmax[kMlpIn];
+};
+
+struct ViscArgs {
+    int nelem, npoin;
+    const int *connec;
+    const float *He, *gpvol, *dlxigp_ip;
+    const int *invAtoIJK, *AtoI, *AtoJ, *AtoK;
+    const float *rho, *u, *p_or_T;
+    float Rgas, gamma, ce, cmax;
+    int normalise;
+    const EntropyStats *stats;
+    const int *only;     // if set: process only elements with only[e] != 0, write nu only
+    float *mu_e, *nu, *numax;
+};
+
+struct FeatureArgs {
+    int nelem, npoin;
+    const int *connec;
+    const float *He, *gpvol;
+    const TableScratch *tabs;
+    const float *rho, *u, *p_or_T;
+    float Rgas, gamma, cmax;
+    const EntropyStats *stats;
+    float *feat, *numax;
+};
+
+cudaError_t launch_entropy_stats(int npoin, const float *rho, const float *p_or_T, float Rgas, float gamma,
+                                 EntropyStats *st, cudaStream_t s);
+cudaError_t launch_entropy_visc(int porder, const ViscArgs &a, cudaStream_t st);
+cudaError_t launch_features(int porder, const FeatureArgs &a, cudaStream_t st);
+cudaError_t launch_mlp_predict(int nelem, const float *feat, const __half *wh, const MlpNorm *nm, const float *numax,
+                               float *y, float *nu, int *flag, cudaStream_t st);
+cudaError_t launch_mlp_norm(int n, const float *feat, MlpNorm *nm, cudaStream_t st);
+cudaError_t launch_mlp_grad(int n, const float *feat, const float *target, const int *idx, int batch, uint32_t seed,
+                            int step, const float *master, const MlpNorm *nm, float *grad, float *loss, cudaStream_t st);
+cudaError_t launch_mlp_adam(float *master, float *m, float *v, float *grad, __half *wh, float lr, int t,
+                            cudaStream_t st);
+cudaError_t launch_mlp_to_half(const float *master, __half *wh, cudaStream_t st);
 
 // Setup kernels.
 template <typename real>

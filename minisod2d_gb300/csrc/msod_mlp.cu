@@ -1,0 +1,429 @@
+// msod_mlp.cu -- learned per-element artificial viscosity.
+//
+// A small per-element network stands in for the entropy-viscosity estimator
+// of msod_visc.cu.  It maps 12 element-local features to y = nu / nu_max in
+// [0, 1]; the learned viscosity is mu_e(e, a) = rho(a) * nu_max(e) * y(e).
+//   network   12 -> 32 -> 32 -> 1, SiLU hidden units, softplus output,
+//             FP16 weights (FP32 master copy while training), FP32 accumulation
+//   training  mean-squared error against the plain estimator's y on
+//             feature -> y pairs, Adam (beta 0.9 / 0.999, eps 1e-8); the forward
+//             pass uses the FP16-rounded weights it will be deployed with
+//   fallback  an element whose features leave the training range [min, max]
+//             (per feature) is flagged; the caller then takes its viscosity
+//             from the plain estimator.
+// Features of element e (nodal values gathered through connec; c = sound
+// speed, s = log(p / rho^gamma) / (gamma - 1), eta = rho s, theta/omega/S =
+// divergence, vorticity and strain-rate norms at the element centre, h =
+// (sum gpvol)^(1/3) / porder, "centre lines" = the three GLL lines through
+// the centre node, n_eta = ||eta - mean eta||_inf over the mesh):
+//   0 (rho_max - rho_min) / rho_mean      1 (p_max - p_min) / p_mean
+//   2 s_max - s_min                       3 mean |u| / mean c
+//   4 max |u| / c                         5 theta h / mean c
+//   6 |omega| h / mean c                  7 |S| h / mean c
+//   8 max over centre lines |rho(0) - 2 rho(mid) + rho(P)| / rho_mean
+//   9 max over centre lines |eta(0) - 2 eta(mid) + eta(P)| / n_eta
+//  10 (eta_max - eta_min) / n_eta
+//  11 max over centre lines of the product-rule defect of eta u_d,
+//     |(eta u)(P) - (eta u)(0) - eta(mid)(u(P) - u(0)) - u(mid)(eta(P) - eta(0))|
+//     / (n_eta (mean |u| + mean c))
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "msod_device.cuh"
+#include "msod_kernels.h"
+
+namespace msod {
+
+__device__ __forceinline__ float silu(float a) { return a / (1.0f + __expf(-a)); }
+__device__ __forceinline__ float sigmoidf_(float a) { return 1.0f / (1.0f + __expf(-a)); }
+__device__ __forceinline__ float softplus(float z) { return z > 20.0f ? z : log1pf(__expf(z)); }
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Features: one warp per element.
+// ---------------------------------------------------------------------------
+template <int P>
+constexpr int feat_warps()
+{
+    return 12288 / (5 * (P + 1) * (P + 1) * (P + 1)) < 8 ? 12288 / (5 * (P + 1) * (P + 1) * (P + 1)) : 8;
+}
+
+template <int P>
+__global__ void __launch_bounds__(32 * feat_warps<P>())
+    features_kernel(int nelem, int npoin, const int *__restrict__ connec, const float *__restrict__ He,
+                    const float *__restrict__ gpvol, const TableScratch *__restrict__ tabs,
+                    const float *__restrict__ rho, const float *__restrict__ u, const float *__restrict__ p_or_T,
+                    float Rgas, float gamma, float cmax, const EntropyStats *__restrict__ st,
+                    float *__restrict__ feat, float *__restrict__ numax_out)
+{
+    constexpr int Q = P + 1, N = Q * Q * Q, kFeatWarps = feat_warps<P>();
+    __shared__ float sv[kFeatWarps][5][N];  // rho, p, u0, u1, u2 by gmsh node
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int e = blockIdx.x * kFeatWarps + w;
+    if (e >= nelem) return;
+    const TableScratch *t = tabs;
+    float rmin = 3e38f, rmax = -3e38f, rsum = 0.f, pmin = 3e38f, pmax = -3e38f, psum = 0.f;
+    float smin = 3e38f, smax = -3e38f, emin = 3e38f, emax = -3e38f, machmax = 0.f, usum = 0.f, csum = 0.f;
+    float spdmax = 0.f, vol = 0.f;
+    const size_t np = (size_t)npoin;
+    for (int a = lane; a < N; a += 32) {
+        int p = ldg(connec + (size_t)a * nelem + e) - 1;
+        p = min(max(p, 0), npoin - 1);
+        const float r = ldg(rho + p);
+        const float pr = Rgas > 0.0f ? r * Rgas * ldg(p_or_T + p) : ldg(p_or_T + p);
+        const float ux = ldg(u + p), uy = ldg(u + np + p), uz = ldg(u + 2 * np + p);
+        sv[w][0][a] = r;
+        sv[w][1][a] = pr;
+        sv[w][2][a] = ux;
+        sv[w][3][a] = uy;
+        sv[w][4][a] = uz;
+        const float c = sqrtf(gamma * pr / r), um = sqrtf(ux * ux + uy * uy + uz * uz);
+        const float s = (logf(pr) - gamma * logf(r)) / (gamma - 1.0f);
+        rmin = fminf(rmin, r); rmax = fmaxf(rmax, r); rsum += r;
+        pmin = fminf(pmin, pr); pmax = fmaxf(pmax, pr); psum += pr;
+        smin = fminf(smin, s); smax = fmaxf(smax, s);
+        emin = fminf(emin, r * s); emax = fmaxf(emax, r * s);
+        machmax = fmaxf(machmax, um / c);
+        usum += um; csum += c;
+        spdmax = fmaxf(spdmax, um + c);
+        vol += ldg(gpvol + (size_t)e * N + a);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        rmin = fminf(rmin, __shfl_xor_sync(~0u, rmin, o)); rmax = fmaxf(rmax, __shfl_xor_sync(~0u, rmax, o));
+        pmin = fminf(pmin, __shfl_xor_sync(~0u, pmin, o)); pmax = fmaxf(pmax, __shfl_xor_sync(~0u, pmax, o));
+        smin = fminf(smin, __shfl_xor_sync(~0u, smin, o)); smax = fmaxf(smax, __shfl_xor_sync(~0u, smax, o));
+        emin = fminf(emin, __shfl_xor_sync(~0u, emin, o)); emax = fmaxf(emax, __shfl_xor_sync(~0u, emax, o));
+        machmax = fmaxf(machmax, __shfl_xor_sync(~0u, machmax, o));
+        spdmax = fmaxf(spdmax, __shfl_xor_sync(~0u, spdmax, o));
+        rsum += __shfl_xor_sync(~0u, rsum, o); psum += __shfl_xor_sync(~0u, psum, o);
+        usum += __shfl_xor_sync(~0u, usum, o); csum += __shfl_xor_sync(~0u, csum, o);
+        vol += __shfl_xor_sync(~0u, vol, o);
+    }
+    __syncwarp();
+    if (lane != 0) return;
+    double mean = st->sum / (double)npoin;
+    double lo = (double)key2f(st->kmin), hi = (double)key2f(st->kmax);
+    float neta = (float)fmax(hi - mean, mean - lo);
+    if (!(neta > 0.0f)) neta = 1.0f;
+    const float rmean = rsum / N, pmean = psum / N, umean = usum / N, cmean = csum / N;
+    const float h = cbrtf(vol) / (float)P;
+    // Centre node and the natural -> SOD 1-D index map (0 -> 0, P -> 1, k -> k+1).
+    const int mnat = P / 2;
+    const int ms = mnat == 0 ? 0 : (mnat == P ? 1 : mnat + 1);
+    auto node = [&](int I, int J, int K) { return t->perm[(K * Q + J) * Q + I]; };
+    const int nat[3] = {0, ms, 1};  // SOD positions of natural 0, mid, P
+    float d2r = 0.f, d2e = 0.f, defect = 0.f;
+    float gi[3][3];  // iso derivative of u_i along d at the centre
+    for (int d = 0; d < 3; ++d) {
+        float rv[3], ev[3], uv[3];
+        for (int k = 0; k < 3; ++k) {
+            const int I = d == 0 ? nat[k] : ms, J = d == 1 ? nat[k] : ms, K = d == 2 ? nat[k] : ms;
+            const int a = node(I, J, K);
+            const float r = sv[w][0][a], pr = sv[w][1][a];
+            rv[k] = r;
+            ev[k] = r * (logf(pr) - gamma * logf(r)) / (gamma - 1.0f);
+            uv[k] = sv[w][2 + d][a];
+        }
+        d2r = fmaxf(d2r, fabsf(rv[0] - 2.f * rv[1] + rv[2]));
+        d2e = fmaxf(d2e, fabsf(ev[0] - 2.f * ev[1] + ev[2]));
+        const float A = ev[2] * uv[2] - ev[0] * uv[0];
+        const float B = ev[1] * (uv[2] - uv[0]) + uv[1] * (ev[2] - ev[0]);
+        defect = fmaxf(defect, fabsf(A - B));
+        for (int i = 0; i < 3; ++i) {
+            float s = 0.f;
+            for (int c = 0; c < Q; ++c) {
+                const int I = d == 0 ? c : ms, J = d == 1 ? c : ms, K = d == 2 ? c : ms;
+                s = fmaf(t->Df[(d * Q + ms) * Q + c], sv[w][2 + i][node(I, J, K)], s);
+            }
+            gi[i][d] = s;
+        }
+    }
+    const float *hp = He + ((size_t)e * N + node(ms, ms, ms)) * 9;
+    float G[3][3];  // G[i][j] = d u_i / d x_j = sum_k He(j,k) gi[i][k]
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) G[i][j] = ldg(hp + 0 * 3 + j) * gi[i][0] + ldg(hp + 3 + j) * gi[i][1] + ldg(hp + 6 + j) * gi[i][2];
+    const float theta = G[0][0] + G[1][1] + G[2][2];
+    const float w0 = G[2][1] - G[1][2], w1 = G[0][2] - G[2][0], w2 = G[1][0] - G[0][1];
+    float s2 = 0.f;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const float sij = 0.5f * (G[i][j] + G[j][i]);
+            s2 += sij * sij;
+        }
+    const float sc = h / cmean;
+    float *f = feat + (size_t)e * kMlpIn;
+    f[0] = (rmax - rmin) / rmean;
+    f[1] = (pmax - pmin) / pmean;
+    f[2] = smax - smin;
+    f[3] = umean / cmean;
+    f[4] = machmax;
+    f[5] = theta * sc;
+    f[6] = sqrtf(w0 * w0 + w1 * w1 + w2 * w2) * sc;
+    f[7] = sqrtf(s2) * sc;
+    f[8] = d2r / rmean;
+    f[9] = d2e / neta;
+    f[10] = (emax - emin) / neta;
+    f[11] = defect / (neta * (umean + cmean));
+    if (numax_out) numax_out[e] = cmax * h * spdmax;
+}
+
+template <int P>
+cudaError_t features_p(const FeatureArgs &a, cudaStream_t st)
+{
+    constexpr int kFeatWarps = feat_warps<P>();
+    const unsigned grid = (unsigned)((a.nelem + kFeatWarps - 1) / kFeatWarps);
+    features_kernel<P><<<grid, 32 * kFeatWarps, 0, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.tabs, a.rho,
+                                                         a.u, a.p_or_T, a.Rgas, a.gamma, a.cmax, a.stats, a.feat,
+                                                         a.numax);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Network
+// ---------------------------------------------------------------------------
+struct Act {
+    float x[kMlpIn], a1[kMlpH], h1[kMlpH], a2[kMlpH], h2[kMlpH], z, y;
+};
+
+// Forward pass with weights w (FP16-rounded values in FP32 registers).
+__device__ __forceinline__ void mlp_forward(const float *__restrict__ w, const MlpNorm &nm, const float *x_raw,
+                                            Act &s)
+{
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) s.x[k] = (x_raw[k] - nm.mean[k]) * nm.inv_std[k];
+    for (int j = 0; j < kMlpH; ++j) {
+        float acc = w[kOffB1 + j];
+#pragma unroll
+        for (int k = 0; k < kMlpIn; ++k) acc = fmaf(w[kOffW1 + j * kMlpIn + k], s.x[k], acc);
+        s.a1[j] = acc;
+        s.h1[j] = silu(acc);
+    }
+    for (int j = 0; j < kMlpH; ++j) {
+        float acc = w[kOffB2 + j];
+        for (int k = 0; k < kMlpH; ++k) acc = fmaf(w[kOffW2 + j * kMlpH + k], s.h1[k], acc);
+        s.a2[j] = acc;
+        s.h2[j] = silu(acc);
+    }
+    float z = w[kOffB3];
+    for (int j = 0; j < kMlpH; ++j) z = fmaf(w[kOffW3 + j], s.h2[j], z);
+    s.z = z;
+    s.y = softplus(z);
+}
+
+// Inference: y in [0, 1] and the out-of-range flag per element.
+__global__ void mlp_predict_kernel(int nelem, const float *__restrict__ feat, const __half *__restrict__ wh,
+                                   const MlpNorm *__restrict__ nm, const float *__restrict__ numax,
+                                   float *__restrict__ y, float *__restrict__ nu, int *__restrict__ flag)
+{
+    __shared__ float w[kMlpParams];
+    __shared__ MlpNorm snm;
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) w[i] = __half2float(wh[i]);
+    if (threadIdx.x == 0) snm = *nm;
+    __syncthreads();
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nelem) return;
+    float x[kMlpIn];
+    int out = 0;
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) {
+        x[k] = feat[(size_t)e * kMlpIn + k];
+        if (!(x[k] >= snm.fmin[k] && x[k] <= snm.fmax[k])) out = 1;
+    }
+    Act s;
+    mlp_forward(w, snm, x, s);
+    const float yy = fminf(s.y, 1.0f);
+    y[e] = yy;
+    if (nu) nu[e] = yy * numax[e];
+    if (flag) flag[e] = out;
+}
+
+// Per-feature mean, 1/std, min, max over the training samples (one block per feature).
+__global__ void mlp_norm_kernel(int n, const float *__restrict__ feat, MlpNorm *nm)
+{
+    const int k = blockIdx.x;
+    double s = 0.0, s2 = 0.0;
+    float mn = 3e38f, mx = -3e38f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float v = feat[(size_t)i * kMlpIn + k];
+        s += v;
+        s2 += (double)v * v;
+        mn = fminf(mn, v);
+        mx = fmaxf(mx, v);
+    }
+    __shared__ double ss[256], ss2[256];
+    __shared__ float smn[256], smx[256];
+    ss[threadIdx.x] = s; ss2[threadIdx.x] = s2; smn[threadIdx.x] = mn; smx[threadIdx.x] = mx;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            ss[threadIdx.x] += ss[threadIdx.x + o];
+            ss2[threadIdx.x] += ss2[threadIdx.x + o];
+            smn[threadIdx.x] = fminf(smn[threadIdx.x], smn[threadIdx.x + o]);
+            smx[threadIdx.x] = fmaxf(smx[threadIdx.x], smx[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double mean = ss[0] / n;
+        const double var = ss2[0] / n - mean * mean;
+        nm->mean[k] = (float)mean;
+        nm->inv_std[k] = (float)(1.0 / sqrt(var > 1e-24 ? var : 1e-24));
+        nm->fmin[k] = smn[0];
+        nm->fmax[k] = smx[0];
+    }
+}
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x)
+{
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(~0u, v, o);
+    return v;
+}
+
+// One batch: loss gradient accumulated into grad (sum over the batch of
+// dL/dparam with L = mean squared error).  Sample i of the batch is
+// idx ? idx[i] : hash(seed, step, i) mod n.
+__global__ void __launch_bounds__(256) mlp_grad_kernel(int n, const float *__restrict__ feat,
+                                                       const float *__restrict__ target, const int *__restrict__ idx,
+                                                       int batch, uint32_t seed, int step,
+                                                       const float *__restrict__ master, const MlpNorm *__restrict__ nm,
+                                                       float *__restrict__ grad, float *__restrict__ loss)
+{
+    __shared__ float w[kMlpParams];
+    __shared__ float g[kMlpParams];
+    __shared__ MlpNorm snm;
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) {
+        w[i] = __half2float(__float2half_rn(master[i]));  // deployed FP16 weights
+        g[i] = 0.0f;
+    }
+    if (threadIdx.x == 0) snm = *nm;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < batch;
+    int sidx = 0;
+    if (live) sidx = idx ? idx[i] : (int)(hash32(seed * 0x9E3779B9u ^ hash32((uint32_t)step * 0x85ebca6bu + i)) % (uint32_t)n);
+    float x[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) x[k] = live ? feat[(size_t)sidx * kMlpIn + k] : 0.0f;
+    Act s;
+    mlp_forward(w, snm, x, s);
+    const float t = live ? target[sidx] : 0.0f;
+    const float dy = live ? 2.0f * (s.y - t) / (float)batch : 0.0f;
+    if (loss) {
+        const float l = warp_sum(live ? (s.y - t) * (s.y - t) / (float)batch : 0.0f);
+        if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
+    }
+    const float dz = dy * sigmoidf_(s.z);
+    const int lane = threadIdx.x & 31;
+    auto acc = [&](int off, float v) {
+        v = warp_sum(v);
+        if (lane == 0) atomicAdd(&g[off], v);
+    };
+    acc(kOffB3, dz);
+    float da2[kMlpH];
+    for (int j = 0; j < kMlpH; ++j) {
+        acc(kOffW3 + j, dz * s.h2[j]);
+        const float sg = sigmoidf_(s.a2[j]);
+        da2[j] = dz * w[kOffW3 + j] * sg * (1.0f + s.a2[j] * (1.0f - sg));
+        acc(kOffB2 + j, da2[j]);
+    }
+    for (int j = 0; j < kMlpH; ++j)
+        for (int k = 0; k < kMlpH; ++k) acc(kOffW2 + j * kMlpH + k, da2[j] * s.h1[k]);
+    for (int k = 0; k < kMlpH; ++k) {
+        float dh1 = 0.0f;
+        for (int j = 0; j < kMlpH; ++j) dh1 = fmaf(w[kOffW2 + j * kMlpH + k], da2[j], dh1);
+        const float sg = sigmoidf_(s.a1[k]);
+        const float da1 = dh1 * sg * (1.0f + s.a1[k] * (1.0f - sg));
+        acc(kOffB1 + k, da1);
+#pragma unroll
+        for (int m = 0; m < kMlpIn; ++m) acc(kOffW1 + k * kMlpIn + m, da1 * s.x[m]);
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < kMlpParams; p += blockDim.x) atomicAdd(&grad[p], g[p]);
+}
+
+// Adam step t (1-based) on the FP32 master weights; clears the gradient and
+// refreshes the FP16 copy.
+__global__ void mlp_adam_kernel(float *__restrict__ master, float *__restrict__ m, float *__restrict__ v,
+                                float *__restrict__ grad, __half *__restrict__ wh, float lr, int t)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= kMlpParams) return;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float gr = grad[p];
+    const float mm = b1 * m[p] + (1.0f - b1) * gr;
+    const float vv = b2 * v[p] + (1.0f - b2) * gr * gr;
+    m[p] = mm;
+    v[p] = vv;
+    const float mh = mm / (1.0f - powf(b1, (float)t)), vh = vv / (1.0f - powf(b2, (float)t));
+    const float w = master[p] - lr * mh / (sqrtf(vh) + eps);
+    master[p] = w;
+    wh[p] = __float2half_rn(w);
+    grad[p] = 0.0f;
+}
+
+__global__ void mlp_to_half_kernel(const float *__restrict__ master, __half *__restrict__ wh)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < kMlpParams) wh[p] = __float2half_rn(master[p]);
+}
+
+}  // namespace
+
+cudaError_t launch_features(int porder, const FeatureArgs &a, cudaStream_t st)
+{
+    switch (porder) {
+    case 1: return features_p<1>(a, st);
+    case 2: return features_p<2>(a, st);
+    case 3: return features_p<3>(a, st);
+    case 4: return features_p<4>(a, st);
+    case 5: return features_p<5>(a, st);
+    case 6: return features_p<6>(a, st);
+    case 7: return features_p<7>(a, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_mlp_predict(int nelem, const float *feat, const __half *wh, const MlpNorm *nm, const float *numax,
+                               float *y, float *nu, int *flag, cudaStream_t st)
+{
+    mlp_predict_kernel<<<(nelem + 127) / 128, 128, 0, st>>>(nelem, feat, wh, nm, numax, y, nu, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_norm(int n, const float *feat, MlpNorm *nm, cudaStream_t st)
+{
+    mlp_norm_kernel<<<kMlpIn, 256, 0, st>>>(n, feat, nm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_grad(int n, const float *feat, const float *target, const int *idx, int batch, uint32_t seed,
+                            int step, const float *master, const MlpNorm *nm, float *grad, float *loss, cudaStream_t st)
+{
+    mlp_grad_kernel<<<(batch + 255) / 256, 256, 0, st>>>(n, feat, target, idx, batch, seed, step, master, nm, grad,
+                                                         loss);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_adam(float *master, float *m, float *v, float *grad, __half *wh, float lr, int t,
+                            cudaStream_t st)
+{
+    mlp_adam_kernel<<<(kMlpParams + 255) / 256, 256, 0, st>>>(master, m, v, grad, wh, lr, t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_to_half(const float *master, __half *wh, cudaStream_t st)
+{
+    mlp_to_half_kernel<<<(kMlpParams + 255) / 256, 256, 0, st>>>(master, wh);
+    return cudaGetLastError();
+}
+
+}  // namespace msod

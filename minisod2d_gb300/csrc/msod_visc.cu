@@ -1,0 +1,292 @@
+// msod_visc.cu -- plain entropy-viscosity estimator for mu_e and the element
+// features of the learned estimator.
+//
+// The reference consumes mu_e (elem_diffu.f90:19, mu_e(nelem,ngaus)) but
+// contains no estimator; its numerical parameters name one
+// (mod_numerical_params.f90:22-28: ce = 0.1, cmax = 0.5, cglob = 1,
+// flag_normalise_entropy = 1).  This file writes the entropy-viscosity method
+// of Guermond, Pasquetti & Popov (J. Comput. Phys. 230 (2011) 4248-4267) for
+// one snapshot of the fields:
+//   entropy      eta = rho/(gamma-1) * log(p / rho^gamma)
+//   residual     R = div(eta u) - eta div u - u . grad eta      (per GLL point)
+//                (the entropy equation's residual with the time derivative
+//                replaced by its steady balance -eta div u - u.grad eta; R
+//                vanishes where the discrete entropy flux is resolved and grows
+//                across under-resolved fronts)
+//   normalise    n_eta = || eta - mean(eta) ||_inf over the mesh (cglob = 1)
+//   per element  h = (sum_g gpvol)^(1/3) / porder,
+//                nu_max = cmax h max_e(|u| + c),  c = sqrt(gamma p / rho),
+//                nu_E   = ce h^2 max_e |R| / n_eta,
+//                nu     = min(nu_max, nu_E)
+//   output       mu_e(e, a) = rho(a) nu(e)   in the reference's mu_e layout.
+// The derivatives are one convection-type pass: the same line-parallel sum
+// factorisation as the convection kernel, over eta, eta u and u.
+#include <cuda_runtime.h>
+
+#include "msod_device.cuh"
+#include "msod_kernels.h"
+
+namespace msod {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Entropy statistics over the nodes: sum, min and max of eta.
+// ---------------------------------------------------------------------------
+__global__ void entropy_stats_init(EntropyStats *st)
+{
+    st->sum = 0.0;
+    st->kmin = f2key(3.0e38f);
+    st->kmax = f2key(-3.0e38f);
+}
+
+// p is given directly (pr) or as rho * Rgas * T (Tem with Rgas > 0).
+__global__ void entropy_stats_kernel(int npoin, const float *__restrict__ rho, const float *__restrict__ p_or_T,
+                                     float Rgas, float gamma, EntropyStats *st)
+{
+    float s = 0.0f, mn = 3.0e38f, mx = -3.0e38f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npoin; i += gridDim.x * blockDim.x) {
+        const float r = ldg(rho + i);
+        const float p = Rgas > 0.0f ? r * Rgas * ldg(p_or_T + i) : ldg(p_or_T + i);
+        const float eta = r / (gamma - 1.0f) * (logf(p) - gamma * logf(r));
+        s += eta;
+        mn = fminf(mn, eta);
+        mx = fmaxf(mx, eta);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&st->sum, (double)s);
+        atomicMin(&st->kmin, f2key(mn));
+        atomicMax(&st->kmax, f2key(mx));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Plain estimator: one group of NE elements per block, one thread per line.
+// ---------------------------------------------------------------------------
+enum { V_RHO = 0, V_P, V_U0, V_U1, V_U2, NVF };
+
+template <class G, int DIR>
+__device__ __forceinline__ void residual_pass(const LineThread<G> &lt, const float *__restrict__ sF,
+                                              float *__restrict__ sR, const int *__restrict__ sPerm,
+                                              const float *__restrict__ sD, const float *__restrict__ He, int e,
+                                              float gamma)
+{
+    constexpr int Q = G::Q, QP = G::QP, R = G::R, NPL = G::NPL;
+    constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
+    const int base = lt.el * G::ES + line_off<DIR, Q, QP>(lt.la, lt.lb, 0);
+    float eta[Q], u_[3][Q];
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        const int o = base + c * OST;
+        const float r = sF[V_RHO * NPL + o], p = sF[V_P * NPL + o];
+        eta[c] = r / (gamma - 1.0f) * (logf(p) - gamma * logf(r));
+#pragma unroll
+        for (int i = 0; i < 3; ++i) u_[i][c] = sF[(V_U0 + i) * NPL + o];
+    }
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+        if (!lt.owns(rr)) continue;
+        const int r = lt.r0 + rr;
+        const int a = sPerm[line_lat<DIR, Q>(lt.la, lt.lb, r)];
+        const float *hp = He + ((size_t)e * G::N + a) * 9 + DIR * 3;
+        const float h0 = ldg(hp), h1 = ldg(hp + 1), h2 = ldg(hp + 2);
+        const float hh[3] = {h0, h1, h2};
+        float deta = 0.0f, ddiv = 0.0f, dveta = 0.0f;  // D.eta, sum_i h_i D.(eta u_i), sum_i h_i D.u_i
+        float dv[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int c = 0; c < Q; ++c) {
+            const float d = sD[(DIR * Q + r) * Q + c];
+            deta = fmaf(d, eta[c], deta);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                ddiv = fmaf(d * hh[i], eta[c] * u_[i][c], ddiv);
+                dv[i] = fmaf(d, u_[i][c], dv[i]);
+            }
+        }
+        float own_eta = eta[0], own_u[3] = {u_[0][0], u_[1][0], u_[2][0]};
+#pragma unroll
+        for (int c = 1; c < Q; ++c)
+            if (c == r) {
+                own_eta = eta[c];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) own_u[i] = u_[i][c];
+            }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) dveta = fmaf(hh[i], dv[i], dveta);
+        const float su = own_u[0] * h0 + own_u[1] * h1 + own_u[2] * h2;
+        const float contrib = ddiv - own_eta * dveta - su * deta;
+        const int o = base + r * OST;
+        sR[o] = DIR == 0 ? contrib : sR[o] + contrib;
+    }
+}
+
+template <class G>
+__global__ void __launch_bounds__(G::NT)
+    entropy_visc_kernel(int nelem, int npoin, const int *__restrict__ connec, const float *__restrict__ He,
+                        const float *__restrict__ gpvol, const float *__restrict__ dlxigp_ip,
+                        const int *__restrict__ invAtoIJK, const int *__restrict__ AtoI, const int *__restrict__ AtoJ,
+                        const int *__restrict__ AtoK, const float *__restrict__ rho, const float *__restrict__ u,
+                        const float *__restrict__ p_or_T, float Rgas, float gamma, float ce, float cmax,
+                        int normalise, const EntropyStats *__restrict__ st, const int *__restrict__ only,
+                        float *__restrict__ mu_e, float *__restrict__ nu_out, float *__restrict__ numax_out)
+{
+    constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT, NPL = G::NPL;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *sF = reinterpret_cast<float *>(smem_raw);  // [NVF][NPL]
+    float *sR = sF + NVF * NPL;                        // [NPL]
+    float *sD = sR + NPL;                              // [3][Q][Q]
+    int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);
+    int *sPerm = sNode + NPL;
+    int *sLat = sPerm + N;
+    __shared__ int s_kR[NE], s_kS[NE];
+    __shared__ float s_vol[NE];
+
+    const int tid = threadIdx.x;
+    const int e0 = blockIdx.x * NE;
+    if (only) {  // fallback mode: only groups with a flagged element do any work
+        __shared__ int s_any;
+        if (tid == 0) {
+            int any = 0;
+            for (int el = 0; el < NE; ++el)
+                if (e0 + el < nelem && only[e0 + el]) any = 1;
+            s_any = any;
+        }
+        __syncthreads();
+        if (!s_any) return;
+    }
+    load_element_tables<float, G::P>(invAtoIJK, AtoI, AtoJ, AtoK, dlxigp_ip, sPerm, sLat, sD, tid, NT);
+    if (tid < NE) {
+        s_kR[tid] = 0;
+        s_kS[tid] = 0;
+        s_vol[tid] = 0.0f;
+    }
+    for (int i = tid; i < NE * N; i += NT) {
+        const int el = i % NE, a = i / NE, e = e0 + el;
+        int node = -1;
+        if (e < nelem) {
+            const int v = ldg(connec + (size_t)a * nelem + e) - 1;
+            node = (v >= 0 && v < npoin) ? v : -1;
+        }
+        sNode[el * ES + sLat[a]] = node;
+    }
+    __syncthreads();
+    const size_t np = (size_t)npoin;
+    for (int i = tid; i < NE * N; i += NT) {
+        const int el = i / N, l = i - el * N;
+        const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
+        const int p = sNode[o];
+        float v[NVF] = {1.0f, 1.0f, 0.0f, 0.0f, 0.0f};
+        if (p >= 0) {
+            v[V_RHO] = ldg(rho + p);
+            v[V_P] = Rgas > 0.0f ? v[V_RHO] * Rgas * ldg(p_or_T + p) : ldg(p_or_T + p);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[V_U0 + c] = ldg(u + c * np + p);
+        }
+#pragma unroll
+        for (int c = 0; c < NVF; ++c) sF[c * NPL + o] = v[c];
+    }
+    __syncthreads();
+    const LineThread<G> lt(tid);
+    const int e = e0 + lt.el;
+    const bool live = lt.active && e < nelem;
+    if (live) residual_pass<G, 0>(lt, sF, sR, sPerm, sD, He, e, gamma);
+    __syncthreads();
+    if (live) residual_pass<G, 1>(lt, sF, sR, sPerm, sD, He, e, gamma);
+    __syncthreads();
+    if (live) residual_pass<G, 2>(lt, sF, sR, sPerm, sD, He, e, gamma);
+    __syncthreads();
+    // Element maxima of |R| and |u| + c, element volume.
+    for (int i = tid; i < NE * N; i += NT) {
+        const int el = i / N, l = i - el * N, ee = e0 + el;
+        if (ee >= nelem) continue;
+        const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
+        const float r = sF[V_RHO * NPL + o], p = sF[V_P * NPL + o];
+        const float ux = sF[V_U0 * NPL + o], uy = sF[V_U1 * NPL + o], uz = sF[V_U2 * NPL + o];
+        const float spd = sqrtf(ux * ux + uy * uy + uz * uz) + sqrtf(gamma * p / r);
+        atomicMax(&s_kR[el], __float_as_int(fabsf(sR[o])));
+        atomicMax(&s_kS[el], __float_as_int(spd));
+        atomicAdd(&s_vol[el], ldg(gpvol + (size_t)ee * N + sPerm[l]));
+    }
+    __syncthreads();
+    float neta = 1.0f;
+    if (normalise) {
+        const double mean = st->sum / (double)npoin;
+        const double lo = (double)key2f(st->kmin), hi = (double)key2f(st->kmax);
+        neta = (float)fmax(hi - mean, mean - lo);
+        if (!(neta > 0.0f)) neta = 1.0f;
+    }
+    for (int i = tid; i < NE * N; i += NT) {
+        const int el = i % NE, a = i / NE, ee = e0 + el;
+        if (ee >= nelem) continue;
+        const float h = cbrtf(s_vol[el]) / (float)(Q - 1);
+        const float numax = cmax * h * __int_as_float(s_kS[el]);
+        const float nuE = ce * h * h * __int_as_float(s_kR[el]) / neta;
+        const float nu = fminf(numax, nuE);
+        if (only) {
+            if (a == 0 && only[ee]) nu_out[ee] = nu;
+            continue;
+        }
+        const int o = el * ES + sLat[a];
+        mu_e[(size_t)a * nelem + ee] = sF[V_RHO * NPL + o] * nu;
+        if (a == 0) {
+            if (nu_out) nu_out[ee] = nu;
+            if (numax_out) numax_out[ee] = numax;
+        }
+    }
+}
+
+template <int P>
+using ViscGeom = LineGeom<float, P>;
+
+template <int P>
+cudaError_t visc_p(const ViscArgs &a, cudaStream_t st)
+{
+    using G = ViscGeom<P>;
+    constexpr size_t smem = (size_t)(NVF + 1) * G::NPL * sizeof(float) + 3 * G::Q * G::Q * sizeof(float) +
+                            (size_t)(G::NPL + 2 * G::N) * sizeof(int);
+    static_assert(smem <= 227 * 1024, "shared memory budget");
+    auto kern = entropy_visc_kernel<G>;
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    const unsigned grid = (unsigned)((a.nelem + G::NE - 1) / G::NE);
+    kern<<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.dlxigp_ip, a.invAtoIJK, a.AtoI,
+                                    a.AtoJ, a.AtoK, a.rho, a.u, a.p_or_T, a.Rgas, a.gamma, a.ce, a.cmax, a.normalise,
+                                    a.stats, a.only, a.mu_e, a.nu, a.numax);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_entropy_stats(int npoin, const float *rho, const float *p_or_T, float Rgas, float gamma,
+                                 EntropyStats *st, cudaStream_t s)
+{
+    entropy_stats_init<<<1, 1, 0, s>>>(st);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    int blocks = (npoin + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    entropy_stats_kernel<<<blocks, 256, 0, s>>>(npoin, rho, p_or_T, Rgas, gamma, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_entropy_visc(int porder, const ViscArgs &a, cudaStream_t st)
+{
+    switch (porder) {
+    case 1: return visc_p<1>(a, st);
+    case 2: return visc_p<2>(a, st);
+    case 3: return visc_p<3>(a, st);
+    case 4: return visc_p<4>(a, st);
+    case 5: return visc_p<5>(a, st);
+    case 6: return visc_p<6>(a, st);
+    case 7: return visc_p<7>(a, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace msod

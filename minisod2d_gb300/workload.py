@@ -69,9 +69,28 @@ class HostCase:
         self.mu_e = np.zeros(self.nelem * n, np.float32)
         self.mu_sgs = np.zeros(self.nelem * n, np.float32)
 
+    def with_seed(self, seed):
+        """The same mesh with the fields of another seed."""
+        import copy
+
+        other = copy.copy(self)
+        other.cfg = Config(self.cfg.name, self.cfg.porder, self.cfg.nx, self.cfg.jitter, self.cfg.kind,
+                           self.cfg.nmodes, int(seed), self.cfg.Cp, self.cfg.Pr)
+        other.fields = fem.fields_recipe(self.cfg.kind, self.cfg.nmodes, int(seed), self.npoin, self.coord)
+        return other
+
 
 class DeviceCase:
     """A workload resident on the GPU as torch tensors, metric built on the device."""
+
+    def set_fields(self, host):
+        """Upload the node fields of another HostCase on the same mesh."""
+        import torch
+
+        self.host = host
+        self.cfg = host.cfg
+        for k, v in host.fields.items():
+            getattr(self, k).copy_(torch.from_numpy(v))
 
     def __init__(self, host, device="cuda", dtype=None):
         import torch

@@ -1069,3 +1069,87 @@ int F(orc_full_diffusion_ijk)(int P, int nelem, int npoin, const int *connec, co
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Entropy viscosity (no reference code: the reference consumes mu_e,        */
+/* elem_diffu.f90:19; knobs mod_numerical_params.f90:22-28)                  */
+/* ------------------------------------------------------------------------- */
+
+/* Entropy-viscosity estimator of the library, restated point by point:
+ * eta = rho/(gamma-1) log(p/rho^gamma); R(g) = div(eta u) - eta div u - u.grad eta
+ * with the reference's per-point derivative table; per element
+ * h = (sum gpvol)^(1/3)/P, nu_max = cmax h max(|u|+c), nu_E = ce h^2 max|R| / n_eta,
+ * nu = min(nu_max, nu_E); mu_e(e,a) = rho(a) nu.  n_eta = max|eta - mean eta|
+ * over the nodes (1 when normalise == 0).  nu/numax may be NULL. */
+int F(orc_entropy_viscosity)(int P, int nelem, int npoin, const int *connec, const real *He, const real *gpvol,
+                             const real *dlxigp_ip, const int *invAtoIJK, const int *AtoI, const int *AtoJ,
+                             const int *AtoK, const real *rho, const real *u, const real *pr, real gamma, real ce,
+                             real cmax, int normalise, real *mu_e, real *nu_out, real *numax_out)
+{
+    elem_t elx;
+    if (elem_setup(&elx, P, invAtoIJK, AtoI, AtoJ, AtoK)) return -1;
+    const elem_t *el = &elx;
+    const int n = el->n, Q = el->Q;
+    const int64_t np = npoin;
+    double sum = 0.0, mn = 1e300, mx = -1e300;
+    for (int64_t p = 0; p < np; ++p) {
+        const double eta = (double)(rho[p] / (gamma - (real)1.0) * (log(pr[p]) - gamma * log(rho[p])));
+        sum += eta;
+        if (eta < mn) mn = eta;
+        if (eta > mx) mx = eta;
+    }
+    real neta = (real)1.0;
+    if (normalise) {
+        const double mean = sum / (double)np;
+        neta = (real)fmax(mx - mean, mean - mn);
+        if (!(neta > 0)) neta = (real)1.0;
+    }
+    real *eta = (real *)malloc(sizeof(real) * n), (*ul)[3] = malloc(sizeof(real) * 3 * n), *rl = malloc(sizeof(real) * n);
+    for (int64_t e = 0; e < nelem; ++e) {
+        real vol = 0, rmax = 0, smax = 0;
+        for (int a = 0; a < n; ++a) {
+            const int64_t p = connec[(int64_t)a * nelem + e] - 1;
+            rl[a] = rho[p];
+            for (int d = 0; d < 3; ++d) ul[a][d] = u[d * np + p];
+            eta[a] = rho[p] / (gamma - (real)1.0) * (log(pr[p]) - gamma * log(rho[p]));
+            const real um = sqrt(ul[a][0] * ul[a][0] + ul[a][1] * ul[a][1] + ul[a][2] * ul[a][2]);
+            const real spd = um + sqrt(gamma * pr[p] / rho[p]);
+            if (spd > smax) smax = spd;
+            vol += gpvol[e * n + a];
+        }
+        for (int g = 0; g < n; ++g) {
+            int I = el->AI[g], J = el->AJ[g], K = el->AK[g];
+            real ge[3] = {0, 0, 0}, gu[3][3], gf[3][3];
+            memset(gu, 0, sizeof gu); memset(gf, 0, sizeof gf);
+            for (int ii = 1; ii <= Q; ++ii) {
+                const int b[3] = {INV(el, ii, J, K), INV(el, I, ii, K), INV(el, I, J, ii)};
+                for (int d = 0; d < 3; ++d) {
+                    const real dl = dlxigp_ip[((ii - 1) * 3 + d) * n + g];
+                    ge[d] = ge[d] + dl * eta[b[d]];
+                    for (int i = 0; i < 3; ++i) {
+                        gu[i][d] = gu[i][d] + dl * ul[b[d]][i];
+                        gf[i][d] = gf[i][d] + dl * (eta[b[d]] * ul[b[d]][i]);
+                    }
+                }
+            }
+            real divf = 0, divu = 0, ugrad = 0;
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    divf = divf + HE(e, g, i, j) * gf[i][j];
+                    divu = divu + HE(e, g, i, j) * gu[i][j];
+                    ugrad = ugrad + ul[g][i] * HE(e, g, i, j) * ge[j];
+                }
+            const real R = fabs(divf - eta[g] * divu - ugrad);
+            if (R > rmax) rmax = R;
+        }
+        const real h = cbrt(vol) / (real)P;
+        const real numax = cmax * h * smax;
+        const real nuE = ce * h * h * rmax / neta;
+        const real nu = numax < nuE ? numax : nuE;
+        for (int a = 0; a < n; ++a) mu_e[(int64_t)a * nelem + e] = rl[a] * nu;
+        if (nu_out) nu_out[e] = nu;
+        if (numax_out) numax_out[e] = numax;
+    }
+    free(eta); free(ul); free(rl);
+    return 0;
+}

@@ -183,3 +183,21 @@ def cpu_count():
         return len(os.sched_getaffinity(0))
     except AttributeError:
         return os.cpu_count() or 1
+
+
+def entropy_viscosity(P, nelem, npoin, geom, rho, u, pr, gamma=1.4, ce=0.1, cmax=0.5, normalise=True,
+                      dtype=np.float64):
+    """The library's entropy-viscosity estimator restated point by point: (mu_e, nu, numax)."""
+    g = _prep_geom(geom, dtype)
+    ins = [_c(x, dtype) for x in (rho, u, pr)]
+    n = (P + 1) ** 3
+    mu_e = np.zeros(nelem * n, dtype)
+    nu = np.zeros(nelem, dtype)
+    numax = np.zeros(nelem, dtype)
+    real = C.c_float if np.dtype(dtype) == np.float32 else C.c_double
+    rc = getattr(lib(), "orc_entropy_viscosity" + _sfx(dtype))(
+        *_geom_args(P, nelem, npoin, g, dtype), *[_p(x) for x in ins], real(gamma), real(ce), real(cmax),
+        C.c_int(1 if normalise else 0), _p(mu_e), _p(nu), _p(numax))
+    if rc != 0:
+        raise RuntimeError("orc_entropy_viscosity failed")
+    return mu_e, nu, numax

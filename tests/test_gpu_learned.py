@@ -1,0 +1,158 @@
+"""GPU checks of the entropy-viscosity estimator and of the learned per-element estimator.
+
+* the estimator against the FP64 oracle (relative L2 of nu and mu_e, within
+  the FP32 floor measured the same way as for the residuals);
+* the element features against their numpy restatement;
+* the network's hand-written backward pass against the numpy gradient at the
+  same FP16-rounded weights (relative error <= 1e-4);
+* training reduces the loss; weight files round-trip and a corrupted file
+  is rejected by its CRC;
+* the fallback reproduces the plain estimator on flagged elements;
+* the per-element-viscosity diffusion equals the mu_e-array diffusion.
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from minisod2d_gb300 import capi, learn, workload
+from oracle import oracle as O
+from tests import mlp_ref, refimpl
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(cuda, P=4, nx=3, seed=1, kind=1, jitter=0.05):
+    cfg = workload.Config("t", P, nx, jitter, kind, 8, seed)
+    host = workload.HostCase(cfg)
+    return host, workload.DeviceCase(host, device=cuda)
+
+
+def _geom(dev, dtype=np.float64):
+    t = O.element_tables(dev.cfg.porder, dtype)
+    return dict(t, connec=dev.host.connec, He=dev.He.cpu().numpy().astype(dtype),
+                gpvol=dev.gpvol.cpu().numpy().astype(dtype))
+
+
+@pytest.mark.parametrize("P,nx", [(4, 3), (5, 2), (2, 4)])
+def test_entropy_viscosity_parity(cuda, P, nx):
+    host, dev = _dev(cuda, P, nx)
+    mu, nu, numax = learn.entropy_viscosity(dev)
+    f = host.fields
+    g64, g32 = _geom(dev), _geom(dev, np.float32)
+    m64, n64, x64 = O.entropy_viscosity(P, dev.nelem, dev.npoin, g64, f["rho"], f["u"], f["pr"])
+    m32, n32, x32 = O.entropy_viscosity(P, dev.nelem, dev.npoin, g32, f["rho"], f["u"], f["pr"], dtype=np.float32)
+    floor = refimpl.rel_l2(n32, n64)
+    err = refimpl.rel_l2(nu.cpu().numpy(), n64)
+    print("VISC P=%d nu err64=%.2e floor=%.2e numax err=%.2e" % (
+        P, err, floor, refimpl.rel_l2(numax.cpu().numpy(), x64)))
+    assert refimpl.rel_l2(numax.cpu().numpy(), x64) < 1e-5
+    assert err <= max(1e-4, 2.0 * floor)
+    assert refimpl.rel_l2(mu.cpu().numpy(), m64) <= max(1e-4, 2.0 * floor)
+
+
+def test_features_parity(cuda):
+    host, dev = _dev(cuda)
+    feat, numax = learn.features(dev)
+    f = host.fields
+    F, nm = mlp_ref.features(_geom(dev), _geom(dev), dev.nelem, dev.npoin, f["rho"], f["u"], f["pr"])
+    G = feat.cpu().numpy().reshape(-1, 12)
+    scale = np.abs(F).max(0) + 1e-30
+    assert np.all(np.abs(G - F) <= 1e-4 * scale + 1e-4 * np.abs(F)), np.abs(G - F).max(0) / scale
+    assert refimpl.rel_l2(numax.cpu().numpy(), nm) < 1e-5
+
+
+def test_gradient_matches_numpy(cuda):
+    import torch
+
+    rng = np.random.default_rng(3)
+    m = learn.Mlp(seed=5)
+    w = rng.normal(0, 0.3, mlp_ref.NPARAMS).astype(np.float32)
+    norm = np.concatenate([rng.normal(0, 1, 12), rng.uniform(0.5, 2, 12), -np.ones(12) * 1e30,
+                           np.ones(12) * 1e30]).astype(np.float32)
+    m.set_params(w, norm)
+    x = rng.normal(0, 1, (300, 12)).astype(np.float32)
+    t = rng.uniform(0, 1, 300).astype(np.float32)
+    idx = rng.integers(0, 300, 257).astype(np.int32)
+    g = m.gradient(torch.from_numpy(x).to(cuda).reshape(-1), torch.from_numpy(t).to(cuda),
+                   torch.from_numpy(idx).to(cuda))
+    gr = mlp_ref.gradient(mlp_ref.fp16_round(w), norm, x[idx], t[idx].astype(np.float64))
+    rel = np.linalg.norm(g - gr) / np.linalg.norm(gr)
+    print("MLP gradient rel err %.2e" % rel)
+    assert rel < 1e-4
+    # forward: prediction equals the numpy network on the FP16 weights
+    y, _, flag = m.predict(torch.from_numpy(x).to(cuda).reshape(-1))
+    yr, _ = mlp_ref.forward(mlp_ref.fp16_round(w), norm, x)
+    assert np.allclose(y.cpu().numpy(), np.minimum(yr, 1.0), rtol=1e-4, atol=1e-6)
+    assert int(flag.sum()) == 0
+
+
+def test_training_reduces_loss_and_weight_files(cuda):
+    import torch
+
+    host, dev = _dev(cuda, 4, 6, seed=2)
+    _, nu, numax = learn.entropy_viscosity(dev)
+    feat, _ = learn.features(dev)
+    y = torch.clamp(nu / numax, 0, 1)
+    m = learn.Mlp(seed=1)
+    loss = m.train(feat, y, steps=400, batch=256, lr=1e-3, seed=7)
+    print("MLP training loss %.3e -> %.3e" % (loss[:20].mean(), loss[-20:].mean()))
+    assert loss[-20:].mean() < 0.25 * loss[:20].mean()
+    yp, _, flag = m.predict(feat)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "w.bin")
+        m.save(path)
+        m2 = learn.Mlp(seed=99)
+        m2.load(path)
+        yp2, _, _ = m2.predict(feat)
+        assert torch.equal(yp, yp2)
+        raw = bytearray(open(path, "rb").read())
+        raw[40] ^= 0x01
+        open(path, "wb").write(bytes(raw))
+        with pytest.raises(capi.MsodError) as ei:
+            m2.load(path)
+        assert ei.value.code == capi.MSOD_ERR_BAD_MODEL
+    assert int(flag.sum()) == 0  # training data lie inside the training range
+
+
+def test_fallback_reproduces_plain_estimator(cuda):
+    import torch
+
+    host, dev = _dev(cuda, 4, 3, seed=4)
+    _, nu_plain, numax = learn.entropy_viscosity(dev)
+    m = learn.Mlp(seed=1)
+    w, norm = m.params()
+    # an empty training range: every element falls back
+    norm = norm.copy()
+    norm[24:36] = 1e30
+    norm[36:48] = -1e30
+    m.set_params(None, norm)
+    nu, flag = learn.learned_viscosity(m, dev)
+    assert int(flag.sum()) == dev.nelem
+    assert refimpl.rel_l2(nu.cpu().numpy(), nu_plain.cpu().numpy()) < 1e-6
+    # an unbounded range: no element falls back and nu = y * numax
+    norm[24:36] = -1e30
+    norm[36:48] = 1e30
+    m.set_params(None, norm)
+    nu, flag = learn.learned_viscosity(m, dev)
+    feat, numax2 = learn.features(dev)
+    y, _, _ = m.predict(feat)
+    assert int(flag.sum()) == 0
+    assert torch.allclose(nu, y * numax2, rtol=1e-6)
+
+
+def test_diffusion_nu_equals_mu_array(cuda):
+    import torch
+
+    from minisod2d_gb300 import kernels
+
+    host, dev = _dev(cuda, 4, 3, seed=5)
+    mu, nu, _ = learn.entropy_viscosity(dev)
+    out_nu = [torch.empty_like(x) for x in (dev.Dmass, dev.Dmom, dev.Dener)]
+    learn.diffusion_ijk_nu(dev, nu, out_nu)
+    out_mu = [torch.empty_like(x) for x in out_nu]
+    kernels.full_diffusion_ijk(*dev.geometry(), dev.cfg.Cp, dev.cfg.Pr, dev.rho, dev.u, dev.Tem, dev.mu_fluid, mu,
+                               dev.mu_sgs, *out_mu)
+    for a, b in zip(out_nu, out_mu):
+        assert refimpl.rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
