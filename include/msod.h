@@ -147,6 +147,23 @@ int msod_diffusion_ijk_f64(int porder, int nelem, int npoin, const int *connec, 
                            const double *mu_sgs, double *Rmass, double *Rmom, double *Rener,
                            void *stream);
 
+/* No counterpart in the reference: mixed-precision form of full_convec_ijk.
+ * FP32 fields and geometry as msod_convec_ijk; the 1-D derivative
+ * contractions run on the tensor cores as hi + lo split FP16 (or BF16)
+ * products with FP32 accumulation, after shifting each differentiated
+ * product by its value at one node of the element and scaling it by a power
+ * of two per element and product; the energy-flux assembly and the nodal
+ * scatter-add run in FP64 and the residuals Rmass, Rmom(npoin,3), Rener are
+ * FP64 arrays.  precision: MSOD_PREC_FP16 or MSOD_PREC_BF16.  porder 1..7. */
+#define MSOD_PREC_FP16 0
+#define MSOD_PREC_BF16 1
+int msod_convec_ijk_mixed(int precision, int porder, int nelem, int npoin, const int *connec,
+                          const float *He, const float *gpvol, const float *dlxigp_ip,
+                          const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
+                          const int *gmshAtoK, const float *u, const float *q, const float *rho,
+                          const float *pr, const float *E, double *Rmass, double *Rmom,
+                          double *Rener, void *stream);
+
 /* Validate element tables and connectivity on the device (synchronous):
  * invAtoIJK is a permutation of 1..n consistent with gmshAtoI/J/K,
  * dlxigp_ip has the per-direction 1-D structure, every connec entry lies in

@@ -23,6 +23,8 @@ MSOD_ERR_BAD_MODEL = 8
 MSOD_MAX_PORDER = 8
 MSOD_FIELDS_SMOOTH = 0
 MSOD_FIELDS_SHOCK = 1
+MSOD_PREC_FP16 = 0
+MSOD_PREC_BF16 = 1
 
 _i, _u64, _i64, _f, _d, _p, _sz = C.c_int, C.c_uint64, C.c_int64, C.c_float, C.c_double, C.c_void_p, C.c_size_t
 
@@ -45,6 +47,7 @@ SIGNATURES = {
     "msod_convec_ijk_split": _GEOM + [_p] * 8 + [_p],
     "msod_diffusion_ijk": _GEOM + [_f, _f] + [_p] * 9 + [_p],
     "msod_convec_ijk_f64": _GEOM64 + [_p] * 8 + [_p],
+    "msod_convec_ijk_mixed": [_i] + _GEOM64 + [_p] * 8 + [_p],
     "msod_diffusion_ijk_f64": _GEOM64 + [_d, _d] + [_p] * 9 + [_p],
     "msod_check_element_tables": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
     "msod_check_element_tables_noalloc": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],

@@ -319,6 +319,42 @@ int msod_convec_ijk_f64(int porder, int nelem, int npoin, const int *connec, con
                                gmshAtoK, u, q, rho, pr, E, Rmass, Rmom, Rener, stream);
 }
 
+int msod_convec_ijk_mixed(int precision, int porder, int nelem, int npoin, const int *connec, const float *He,
+                          const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI,
+                          const int *gmshAtoJ, const int *gmshAtoK, const float *u, const float *q, const float *rho,
+                          const float *pr, const float *E, double *Rmass, double *Rmom, double *Rener, void *stream)
+{
+    clear_error();
+    const int prec = precision;
+    if (prec != MSOD_PREC_FP16 && prec != MSOD_PREC_BF16)
+        return set_error(MSOD_ERR_INVALID_ARG, "precision %d is neither MSOD_PREC_FP16 nor MSOD_PREC_BF16", precision);
+    int rc = check_geometry(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
+                            gmshAtoK);
+    if (rc) return rc;
+    if (porder > 7) return set_error(MSOD_ERR_PORDER, "the mixed-precision kernel serves porder 1..7");
+    if (!u || !q || !rho || !pr || !E || !Rmass || !Rmom || !Rener)
+        return set_error(MSOD_ERR_INVALID_ARG, "NULL field or residual array");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (checked_mode()) {
+        rc = run_check(porder, nelem, npoin, connec, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, st);
+        if (rc) return rc;
+    }
+    TableScratch *tabs = device_tables();
+    if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
+    rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
+    if (rc) return rc;
+    ElementArgs<float> ea;
+    ea.nelem = nelem; ea.npoin = npoin; ea.connec = connec; ea.He = He; ea.gpvol = gpvol; ea.dlxigp_ip = dlxigp_ip;
+    ea.invAtoIJK = invAtoIJK; ea.AtoI = gmshAtoI; ea.AtoJ = gmshAtoJ; ea.AtoK = gmshAtoK;
+    MixedConvecArgs a;
+    a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol;
+    a.u = u; a.q = q; a.rho = rho; a.pr = pr; a.E = E; a.Rmass = Rmass; a.Rmom = Rmom; a.Rener = Rener;
+    rc = cuda_status(launch_table_prep<float>(porder, ea, tabs, st), "table preparation launch");
+    if (!rc) rc = cuda_status(launch_convec_mixed(porder, prec, a, tabs, st), "mixed convection launch");
+    if (!rc && checked_mode()) rc = cuda_status(cudaStreamSynchronize(st), "mixed convection kernel");
+    return rc;
+}
+
 int msod_diffusion_ijk_f64(int porder, int nelem, int npoin, const int *connec, const double *He,
                            const double *gpvol, const double *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI,
                            const int *gmshAtoJ, const int *gmshAtoK, double Cp, double Pr, const double *rho,

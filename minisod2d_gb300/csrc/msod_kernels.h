@@ -70,6 +70,18 @@ cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, const Tab
 template <typename real>
 cudaError_t launch_diffu_plain(int porder, const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st);
 
+// Mixed-precision convection: FP32 fields, FP64 residuals (zeroed by the
+// caller; tables prepared).  precision: MSOD_PREC_FP16 or MSOD_PREC_BF16.
+struct MixedConvecArgs {
+    int nelem, npoin;
+    const int *connec;
+    const float *He, *gpvol;
+    const float *u, *q, *rho, *pr, *E;
+    double *Rmass, *Rmom, *Rener;
+};
+cudaError_t launch_convec_mixed(int porder, int precision, const MixedConvecArgs &a,
+                                const TableScratch *tabs, cudaStream_t st);
+
 // ---------------------------------------------------------------------------
 // Entropy viscosity and the learned estimator
 // ---------------------------------------------------------------------------

@@ -192,7 +192,7 @@ int msod_mlp_create(msod_mlp **out, uint64_t seed)
     fill(kOffW1, kMlpH, kMlpIn);
     fill(kOffW2, kMlpH, kMlpH);
     fill(kOffW3, 1, kMlpH);
-    w[kOffB3] = -2.0f;
+    w[kOffB3] = 5.0f;  // s = 5 decades: y = 1e-5 before training
     MlpNorm nm;
     for (int k = 0; k < kMlpIn; ++k) { nm.mean[k] = 0.f; nm.inv_std[k] = 1.f; nm.fmin[k] = -3e38f; nm.fmax[k] = 3e38f; }
     int rc = cuda_rc(cudaMemcpy(m->master, w.data(), nf * sizeof(float), cudaMemcpyHostToDevice), "cudaMemcpy");

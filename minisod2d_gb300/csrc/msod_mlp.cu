@@ -2,12 +2,17 @@
 //
 // A small per-element network stands in for the entropy-viscosity estimator
 // of msod_visc.cu.  It maps 12 element-local features to y = nu / nu_max in
-// [0, 1]; the learned viscosity is mu_e(e, a) = rho(a) * nu_max(e) * y(e).
+// (0, 1]; the learned viscosity is mu_e(e, a) = rho(a) * nu_max(e) * y(e).
+// The plain estimator's y spans many decades (entropy viscosity far below
+// the first-order bound away from under-resolved fronts), so the network
+// works in decades: its softplus output s >= 0 gives y = 10^-s, and the
+// heavy-tailed features enter as logarithms.
 //   network   12 -> 32 -> 32 -> 1, SiLU hidden units, softplus output,
 //             FP16 weights (FP32 master copy while training), FP32 accumulation
-//   training  mean-squared error against the plain estimator's y on
-//             feature -> y pairs, Adam (beta 0.9 / 0.999, eps 1e-8); the forward
-//             pass uses the FP16-rounded weights it will be deployed with
+//   training  mean-squared error of s against -log10 of the plain estimator's
+//             y (clamped to [1e-12, 1]) on feature -> y pairs, Adam (beta
+//             0.9 / 0.999, eps 1e-8); the forward pass uses the FP16-rounded
+//             weights it will be deployed with
 //   fallback  an element whose features leave the training range [min, max]
 //             (per feature) is flagged; the caller then takes its viscosity
 //             from the plain estimator.
@@ -15,7 +20,8 @@
 // speed, s = log(p / rho^gamma) / (gamma - 1), eta = rho s, theta/omega/S =
 // divergence, vorticity and strain-rate norms at the element centre, h =
 // (sum gpvol)^(1/3) / porder, "centre lines" = the three GLL lines through
-// the centre node, n_eta = ||eta - mean eta||_inf over the mesh):
+// the centre node, n_eta = ||eta - mean eta||_inf over the mesh; every
+// feature except 3, 4 and 5 is stored as log(max(v, 0) + 1e-12)):
 //   0 (rho_max - rho_min) / rho_mean      1 (p_max - p_min) / p_mean
 //   2 s_max - s_min                       3 mean |u| / mean c
 //   4 max |u| / c                         5 theta h / mean c
@@ -37,6 +43,12 @@ namespace msod {
 __device__ __forceinline__ float silu(float a) { return a / (1.0f + __expf(-a)); }
 __device__ __forceinline__ float sigmoidf_(float a) { return 1.0f / (1.0f + __expf(-a)); }
 __device__ __forceinline__ float softplus(float z) { return z > 20.0f ? z : log1pf(__expf(z)); }
+// Heavy-tailed non-negative features enter as logarithms (offset 1e-12).
+__device__ __forceinline__ float flog(float v) { return logf(fmaxf(v, 0.0f) + 1e-12f); }
+// The network's output s >= 0 is a number of decades: y = 10^-s.  Targets y
+// are mapped to s = -log10(max(y, 1e-12)) for the loss.
+__device__ __forceinline__ float y_from_s(float s) { return exp10f(-s); }
+__device__ __forceinline__ float s_from_y(float y) { return -log10f(fminf(fmaxf(y, 1e-12f), 1.0f)); }
 
 namespace {
 
@@ -154,18 +166,18 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
         }
     const float sc = h / cmean;
     float *f = feat + (size_t)e * kMlpIn;
-    f[0] = (rmax - rmin) / rmean;
-    f[1] = (pmax - pmin) / pmean;
-    f[2] = smax - smin;
+    f[0] = flog((rmax - rmin) / rmean);
+    f[1] = flog((pmax - pmin) / pmean);
+    f[2] = flog(smax - smin);
     f[3] = umean / cmean;
     f[4] = machmax;
     f[5] = theta * sc;
-    f[6] = sqrtf(w0 * w0 + w1 * w1 + w2 * w2) * sc;
-    f[7] = sqrtf(s2) * sc;
-    f[8] = d2r / rmean;
-    f[9] = d2e / neta;
-    f[10] = (emax - emin) / neta;
-    f[11] = defect / (neta * (umean + cmean));
+    f[6] = flog(sqrtf(w0 * w0 + w1 * w1 + w2 * w2) * sc);
+    f[7] = flog(sqrtf(s2) * sc);
+    f[8] = flog(d2r / rmean);
+    f[9] = flog(d2e / neta);
+    f[10] = flog((emax - emin) / neta);
+    f[11] = flog(defect / (neta * (umean + cmean)));
     if (numax_out) numax_out[e] = cmax * h * spdmax;
 }
 
@@ -212,7 +224,7 @@ __device__ __forceinline__ void mlp_forward(const float *__restrict__ w, const M
     s.y = softplus(z);
 }
 
-// Inference: y in [0, 1] and the out-of-range flag per element.
+// Inference: y = 10^-s in (0, 1] and the out-of-range flag per element.
 __global__ void mlp_predict_kernel(int nelem, const float *__restrict__ feat, const __half *__restrict__ wh,
                                    const MlpNorm *__restrict__ nm, const float *__restrict__ numax,
                                    float *__restrict__ y, float *__restrict__ nu, int *__restrict__ flag)
@@ -233,7 +245,7 @@ __global__ void mlp_predict_kernel(int nelem, const float *__restrict__ feat, co
     }
     Act s;
     mlp_forward(w, snm, x, s);
-    const float yy = fminf(s.y, 1.0f);
+    const float yy = y_from_s(s.y);
     y[e] = yy;
     if (nu) nu[e] = yy * numax[e];
     if (flag) flag[e] = out;
@@ -315,7 +327,7 @@ __global__ void __launch_bounds__(256) mlp_grad_kernel(int n, const float *__res
     for (int k = 0; k < kMlpIn; ++k) x[k] = live ? feat[(size_t)sidx * kMlpIn + k] : 0.0f;
     Act s;
     mlp_forward(w, snm, x, s);
-    const float t = live ? target[sidx] : 0.0f;
+    const float t = live ? s_from_y(target[sidx]) : 0.0f;
     const float dy = live ? 2.0f * (s.y - t) / (float)batch : 0.0f;
     if (loss) {
         const float l = warp_sum(live ? (s.y - t) * (s.y - t) / (float)batch : 0.0f);

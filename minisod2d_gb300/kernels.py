@@ -109,6 +109,24 @@ def full_diffusion_ijk(nelem, npoin, connec, Ngp, dNgp, He, gpvol, dlxigp_ip, xg
         raise TypeError("He must be float32 or float64")
 
 
+def full_convec_ijk_mixed(nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                          u, q, rho, pr, E, Rmass, Rmom, Rener, precision="fp16", stream=None):
+    """Mixed-precision form of elem_convec.f90:198: FP32 fields, FP64 residuals.
+
+    ``precision`` is "fp16" or "bf16" (hi + lo split tensor-core contractions).
+    """
+    import torch
+
+    P, g = _geometry(nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                     torch.float32)
+    f = [_ptr(u, "u", torch.float32, 3 * npoin), _ptr(q, "q", torch.float32, 3 * npoin),
+         _ptr(rho, "rho", torch.float32, npoin), _ptr(pr, "pr", torch.float32, npoin),
+         _ptr(E, "E", torch.float32, npoin), _ptr(Rmass, "Rmass", torch.float64, npoin),
+         _ptr(Rmom, "Rmom", torch.float64, 3 * npoin), _ptr(Rener, "Rener", torch.float64, npoin)]
+    prec = {"fp16": capi.MSOD_PREC_FP16, "bf16": capi.MSOD_PREC_BF16}[precision]
+    capi.call("msod_convec_ijk_mixed", prec, P, nelem, npoin, *g, *f, _stream(stream))
+
+
 def elem_jacobian(porder, nelem, npoin, connec, coord, dNgp, wgp, gpvol, He, stream=None):
     """jacobian_oper.f90:7 on the device; writes gpvol and He in place."""
     import torch
@@ -138,5 +156,5 @@ def set_checked(enabled):
     capi.call("msod_set_checked", 1 if enabled else 0)
 
 
-__all__ = ["full_convec_ijk", "full_convec_ijk_split", "full_diffusion_ijk", "elem_jacobian",
+__all__ = ["full_convec_ijk", "full_convec_ijk_split", "full_diffusion_ijk", "full_convec_ijk_mixed", "elem_jacobian",
            "check_element_tables", "set_checked"]

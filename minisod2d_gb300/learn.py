@@ -156,3 +156,169 @@ def training_data(cfg, seeds, device="cuda"):
         ys.append(torch.clamp(nu / torch.clamp(numax, min=1e-30), 0.0, 1.0))
         feats.append(f.clone())
     return torch.cat(feats), torch.cat(ys)
+
+
+def _event_ms(fn, reps):
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    b.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def _mu_from_nu(dev, nu):
+    """mu_e(nelem, ngaus) = rho(node) * nu(element) in the reference's layout."""
+    import torch
+
+    n = dev.cfg.nnode
+    node = dev.connec.view(n, dev.nelem).long() - 1
+    return (dev.rho[node] * nu.view(1, -1)).reshape(-1)
+
+
+def evaluate(mlp, dev, ybar=None, reps=5):
+    """Learned against plain estimator on one field instance: errors, fallback, times.
+
+    ``ybar`` (the training targets' mean y) adds the constant-ratio
+    estimator nu = ybar * nu_max, the best feature-free choice in L2."""
+    import torch
+
+    from . import kernels
+
+    mu_p, nu_p, numax = entropy_viscosity(dev)
+    out_p = [torch.empty_like(x) for x in (dev.Dmass, dev.Dmom, dev.Dener)]
+    kernels.full_diffusion_ijk(*dev.geometry(), dev.cfg.Cp, dev.cfg.Pr, dev.rho, dev.u, dev.Tem, dev.mu_fluid, mu_p,
+                               dev.mu_sgs, *out_p)
+    nu_l, flag = learned_viscosity(mlp, dev)
+    out_l = [torch.empty_like(x) for x in out_p]
+    diffusion_ijk_nu(dev, nu_l, out_l)
+
+    def rel(a, b):
+        return float(torch.linalg.vector_norm((a - b).double()) / max(torch.linalg.vector_norm(b.double()), 1e-300))
+
+    # Two estimators that need no entropy residual, for comparison: the
+    # first-order bound nu_max everywhere, and nu_max times the mean training ratio.
+    out_b = [torch.empty_like(x) for x in out_p]
+    diffusion_ijk_nu(dev, numax, out_b)
+    r = {
+        "nu_rel_l2": rel(nu_l, nu_p),
+        "mu_e_rel_l2": rel(_mu_from_nu(dev, nu_l), mu_p),
+        "Rmass_rel_l2": rel(out_l[0], out_p[0]),
+        "Rmom_rel_l2": rel(out_l[1], out_p[1]),
+        "Rener_rel_l2": rel(out_l[2], out_p[2]),
+        "fallback_fraction": float(flag.float().mean()),
+        "numax_everywhere": {"nu_rel_l2": rel(numax, nu_p), "Rmom_rel_l2": rel(out_b[1], out_p[1]),
+                             "Rener_rel_l2": rel(out_b[2], out_p[2])},
+    }
+    if ybar is not None:
+        nu_c = float(ybar) * numax
+        diffusion_ijk_nu(dev, nu_c, out_b)
+        r["constant_ratio"] = {"nu_rel_l2": rel(nu_c, nu_p), "Rmom_rel_l2": rel(out_b[1], out_p[1]),
+                               "Rener_rel_l2": rel(out_b[2], out_p[2])}
+    diffusion_ijk_nu(dev, torch.zeros_like(numax), out_b)
+    r["no_artificial_viscosity"] = {"nu_rel_l2": 1.0, "Rmom_rel_l2": rel(out_b[1], out_p[1]),
+                                    "Rener_rel_l2": rel(out_b[2], out_p[2])}
+    mu_buf, nu_buf, nm_buf = torch.empty_like(mu_p), torch.empty_like(nu_p), torch.empty_like(numax)
+    nu_lb, flag_b = torch.empty_like(nu_l), torch.empty_like(flag)
+
+    def plain():
+        entropy_viscosity(dev, mu_buf, nu_buf, nm_buf)
+        kernels.full_diffusion_ijk(*dev.geometry(), dev.cfg.Cp, dev.cfg.Pr, dev.rho, dev.u, dev.Tem, dev.mu_fluid,
+                                   mu_buf, dev.mu_sgs, *out_p)
+
+    def learned():
+        learned_viscosity(mlp, dev, nu_lb, flag_b)
+        diffusion_ijk_nu(dev, nu_lb, out_l)
+
+    r["ms_plain_estimator"] = _event_ms(lambda: entropy_viscosity(dev, mu_buf, nu_buf, nm_buf), reps)
+    r["ms_learned_estimator"] = _event_ms(lambda: learned_viscosity(mlp, dev, nu_lb, flag_b), reps)
+    r["ms_plain_estimator_plus_diffusion"] = _event_ms(plain, reps)
+    r["ms_learned_estimator_plus_diffusion"] = _event_ms(learned, reps)
+    return r
+
+
+def train_and_evaluate(cfg, train_seeds, eval_seeds, steps=2000, batch=4096, lr=1e-3, seed=0, weights=None,
+                       device="cuda"):
+    """Train the network on the plain estimator's output over ``train_seeds``
+    and evaluate it on ``eval_seeds`` (the same mesh, other field instances).
+    Returns a report dict; writes the weight file if ``weights`` is given."""
+    import time
+
+    import torch
+
+    t0 = time.time()
+    feat, y = training_data(cfg, train_seeds, device=device)
+    t_data = time.time() - t0
+    mlp = Mlp(seed=seed)
+    t0 = time.time()
+    loss = mlp.train(feat, y, steps=steps, batch=batch, lr=lr, seed=seed)
+    t_train = time.time() - t0
+    ybar = float(y.double().mean())
+    del feat, y
+    torch.cuda.empty_cache()
+    if weights:
+        mlp.save(weights)
+    host = workload.HostCase(workload.Config(cfg.name, cfg.porder, cfg.nx, cfg.jitter, cfg.kind, cfg.nmodes,
+                                             int(eval_seeds[0])))
+    dev = workload.DeviceCase(host, device=device)
+    per_seed = []
+    for s in eval_seeds:
+        if s != eval_seeds[0]:
+            host = host.with_seed(int(s))
+            dev.set_fields(host)
+        per_seed.append(dict(seed=int(s), **evaluate(mlp, dev, ybar)))
+
+    def mean(key, sub=None):
+        v = [(p[sub][key] if sub else p[key]) for p in per_seed]
+        return float(np.mean(v))
+
+    keys = ("nu_rel_l2", "mu_e_rel_l2", "Rmass_rel_l2", "Rmom_rel_l2", "Rener_rel_l2", "fallback_fraction",
+            "ms_plain_estimator", "ms_learned_estimator", "ms_plain_estimator_plus_diffusion",
+            "ms_learned_estimator_plus_diffusion")
+    summary = {k: mean(k) for k in keys}
+    for sub in ("numax_everywhere", "constant_ratio", "no_artificial_viscosity"):
+        summary[sub] = {k: mean(k, sub) for k in per_seed[0][sub]}
+    summary["time_saved_fraction"] = 1.0 - summary["ms_learned_estimator_plus_diffusion"] / \
+        summary["ms_plain_estimator_plus_diffusion"]
+    return {
+        "workload": cfg.name, "porder": cfg.porder, "nelem": cfg.nelem, "npoin": cfg.npoin,
+        "train_seeds": [int(s) for s in train_seeds], "eval_seeds": [int(s) for s in eval_seeds],
+        "steps": steps, "batch": batch, "lr": lr, "samples": int(len(train_seeds) * cfg.nelem), "ybar": ybar,
+        "loss_first_50": float(loss[:50].mean()), "loss_last_50": float(loss[-50:].mean()),
+        "seconds_data": t_data, "seconds_train": t_train,
+        "mean": summary, "per_seed": per_seed,
+    }
+
+
+def _main(argv=None):
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="Train the per-element viscosity network and evaluate it.")
+    ap.add_argument("--config", default="learned_48")
+    ap.add_argument("--ntrain", type=int, default=64)
+    ap.add_argument("--neval", type=int, default=16)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--weights", default=None)
+    ap.add_argument("--report", default=None)
+    a = ap.parse_args(argv)
+    cfg = workload.CONFIGS[a.config]
+    train = list(range(a.ntrain))
+    ev = list(range(1000, 1000 + a.neval))
+    rep = train_and_evaluate(cfg, train, ev, a.steps, a.batch, a.lr, weights=a.weights)
+    txt = json.dumps(rep, indent=1)
+    if a.report:
+        with open(a.report, "w") as f:
+            f.write(txt + "\n")
+    print(json.dumps(rep["mean"], indent=1))
+
+
+if __name__ == "__main__":
+    _main()

@@ -147,6 +147,22 @@ class DeviceCase:
                                 self.Rener, stream=stream, split=split)
         return self.Rmass, self.Rmom, self.Rener
 
+    def convec_mixed(self, precision="fp16", out=None, stream=None):
+        """Mixed-precision convection into FP64 residuals (allocated unless ``out`` is given)."""
+        import torch
+
+        from . import kernels
+
+        if out is None:
+            dev = self.He.device
+            out = (torch.empty(self.npoin, dtype=torch.float64, device=dev),
+                   torch.empty(3 * self.npoin, dtype=torch.float64, device=dev),
+                   torch.empty(self.npoin, dtype=torch.float64, device=dev))
+        g = self.geometry()
+        kernels.full_convec_ijk_mixed(g[0], g[1], g[2], g[5], g[6], g[7], *g[9:], self.u, self.q, self.rho, self.pr,
+                                      self.E, *out, precision=precision, stream=stream)
+        return out
+
     def diffu(self, stream=None):
         from . import kernels
 

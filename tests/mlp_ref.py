@@ -29,8 +29,35 @@ def sig(a):
     return 1.0 / (1.0 + np.exp(-a))
 
 
+# Features stored as log(max(v, 0) + 1e-12); the others (mean Mach, max Mach,
+# scaled divergence) stay linear.
+LOG_FEATURES = [0, 1, 2, 6, 7, 8, 9, 10, 11]
+
+
+def log_features(F):
+    G = np.array(F, np.float64, copy=True)
+    G[:, LOG_FEATURES] = np.log(np.maximum(G[:, LOG_FEATURES], 0.0) + 1e-12)
+    return G
+
+
+def raw_features(G):
+    F = np.array(G, np.float64, copy=True)
+    F[:, LOG_FEATURES] = np.exp(F[:, LOG_FEATURES]) - 1e-12
+    return F
+
+
+def s_from_y(y):
+    """Training target of the network's output: decades below the bound."""
+    return -np.log10(np.clip(np.asarray(y, np.float64), 1e-12, 1.0))
+
+
+def y_from_s(s):
+    return 10.0 ** (-np.asarray(s, np.float64))
+
+
 def forward(w, norm, x):
-    """x: (B, 12) raw features; norm: 48 floats (mean, 1/std, min, max). Returns y and the activations."""
+    """x: (B, 12) features as stored; norm: 48 floats (mean, 1/std, min, max).
+    Returns the softplus output s (y = 10^-s) and the activations."""
     W1, b1, W2, b2, W3, b3 = unpack(w)
     mean, inv_std = np.asarray(norm[:NIN], np.float64), np.asarray(norm[NIN:2 * NIN], np.float64)
     xh = (np.asarray(x, np.float64) - mean) * inv_std
@@ -44,9 +71,10 @@ def forward(w, norm, x):
 
 
 def gradient(w, norm, x, t):
-    """d/dw of mean((y - t)^2) over the batch (flattened like the device layout)."""
+    """d/dw of mean((s - s_from_y(t))^2) over the batch (flattened like the device layout)."""
     W1, b1, W2, b2, W3, b3 = unpack(w)
     y, (xh, a1, h1, a2, h2, z) = forward(w, norm, x)
+    t = s_from_y(t)
     B = len(t)
     dz = 2.0 * (y - t) / B * sig(z)
     gW3 = dz @ h2
@@ -71,7 +99,7 @@ def gradient(w, norm, x, t):
 
 def loss(w, norm, x, t):
     y, _ = forward(w, norm, x)
-    return float(np.mean((y - t) ** 2))
+    return float(np.mean((y - s_from_y(t)) ** 2))
 
 
 def features(tables, geom, nelem, npoin, rho, u, pr, gamma=1.4, cmax=0.5):

@@ -1,0 +1,98 @@
+"""GPU checks of the mixed-precision convection (FP16 / BF16 hi + lo tensor-core
+contractions, FP64 scatter and energy-flux assembly).
+
+Reference: the FP64 oracle on the same inputs (the FP32 fields and geometry
+the kernel reads, promoted to FP64).  Criterion per residual: relative L2
+<= 1e-4 for both formats, and <= 1e-5 for FP16 (whose split carries about 22
+bits of each product's variation over the element).  The plain FP32 GPU
+kernel's distance from the same FP64 answer (the FP32 floor) is printed
+beside it.
+"""
+import numpy as np
+import pytest
+
+from minisod2d_gb300 import workload
+from oracle import oracle as O
+from tests import refimpl
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+TOL_FP16 = 1e-5
+
+
+def _case(cuda, P, nx, kind=0, nmodes=8, seed=0, jitter=0.05):
+    cfg = workload.Config("t", P, nx, jitter, kind, nmodes, seed)
+    host = workload.HostCase(cfg)
+    return host, workload.DeviceCase(host, device=cuda)
+
+
+def _oracle64(host, dev):
+    t = host.tables
+    geom = dict(t, connec=host.connec, He=dev.He.cpu().numpy(), gpvol=dev.gpvol.cpu().numpy())
+    f = host.fields
+    return O.full_convec_ijk(dev.cfg.porder, dev.nelem, dev.npoin, geom, f["u"], f["q"], f["rho"], f["pr"], f["E"],
+                             dtype=np.float64, nthreads=8)
+
+
+def _errs(gpu, ref):
+    return [refimpl.rel_l2(g.cpu().numpy().astype(np.float64), r) for g, r in zip(gpu, ref)]
+
+
+@pytest.mark.parametrize("P,nx,kind,nmodes", [(7, 3, 0, 16), (5, 4, 1, 8), (4, 4, 0, 8), (2, 5, 1, 8)])
+def test_mixed_convection_vs_fp64_oracle(cuda, P, nx, kind, nmodes):
+    host, dev = _case(cuda, P, nx, kind, nmodes)
+    ref = _oracle64(host, dev)
+    floor = _errs(dev.convec(), ref)
+    for prec in ("fp16", "bf16"):
+        errs = _errs(dev.convec_mixed(prec), ref)
+        print("MIXED P=%d kind=%d %s err=%s floor32=%s" % (
+            P, kind, prec, ["%.2e" % x for x in errs], ["%.2e" % x for x in floor]))
+        for name, e, fl in zip(("mass", "mom", "ener"), errs, floor):
+            assert e <= TOL, (prec, name, e)
+            if prec == "fp16":
+                assert e <= TOL_FP16, (prec, name, e, fl)
+
+
+def test_mixed_convection_deterministic_inputs_and_intent_out(cuda):
+    import torch
+
+    host, dev = _case(cuda, 7, 2, 0, 16, seed=3)
+    a = dev.convec_mixed("fp16")
+    out = tuple(torch.full_like(x, 7.0) for x in a)
+    b = dev.convec_mixed("fp16", out=out)
+    for x, y in zip(a, b):
+        # atomics reorder the per-node sums; values agree to rounding
+        assert refimpl.rel_l2(x.cpu().numpy(), y.cpu().numpy()) < 1e-12
+
+
+def test_mixed_convection_constant_fields_give_zero(cuda):
+    """Constant fields: every derivative vanishes exactly (the shift by the
+    reference node makes the split inputs exactly zero)."""
+    import torch
+
+    host, dev = _case(cuda, 5, 3, 0, 8)
+    for t, v in ((dev.rho, 1.25), (dev.pr, 0.8), (dev.E, 2.5)):
+        t.fill_(v)
+    dev.u.fill_(0.3)
+    dev.q.fill_(0.375)
+    for prec in ("fp16", "bf16"):
+        for x in dev.convec_mixed(prec):
+            assert float(torch.abs(x).max()) == 0.0
+
+
+def test_mixed_rejects_bad_arguments(cuda):
+    import torch
+
+    from minisod2d_gb300 import capi, kernels
+
+    host, dev = _case(cuda, 4, 2)
+    out = dev.convec_mixed("fp16")
+    g = dev.geometry()
+    args = [g[0], g[1], g[2], g[5], g[6], g[7], *g[9:], dev.u, dev.q, dev.rho, dev.pr, dev.E]
+    with pytest.raises(TypeError):
+        kernels.full_convec_ijk_mixed(*args, dev.Rmass, dev.Rmom, dev.Rener)  # FP32 outputs
+    with pytest.raises(capi.MsodError) as ei:
+        capi.call("msod_convec_ijk_mixed", 5, 4, dev.nelem, dev.npoin, *[t.data_ptr() for t in args[2:]],
+                  *[t.data_ptr() for t in out], torch.cuda.current_stream().cuda_stream)
+    assert ei.value.code == capi.MSOD_ERR_INVALID_ARG
