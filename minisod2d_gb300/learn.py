@@ -16,6 +16,9 @@ import numpy as np
 from . import capi, workload
 
 GAMMA, RGAS, CE, CMAX = 1.4, 287.0, 0.1, 0.5
+# Network trained on the learned_48 workload (48^3 hexes, porder 4, shock-like
+# fields, 64 training seeds; python -m minisod2d_gb300.learn writes it).
+SHIPPED_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "mlp_learned_48.bin")
 NFEAT = 12
 NPARAMS = 1505
 

@@ -181,3 +181,24 @@ def test_network_gains_over_estimators_without_entropy_residual(cuda):
         for alt in ("numax_everywhere", "constant_ratio", "no_artificial_viscosity"):
             assert m[k] < 0.5 * m[alt][k], (k, alt)
     assert m["fallback_fraction"] < 0.5
+
+
+def test_shipped_network_on_held_out_learned_48_seed(cuda):
+    """The committed network (trained on 64 seeds of the 48^3 shock workload)
+    on a seed it never saw: close to the plain estimator, far closer than the
+    best constant fraction of nu_max, few fallbacks."""
+    cfg = workload.CONFIGS["learned_48"]
+    host = workload.HostCase(workload.Config(cfg.name, cfg.porder, cfg.nx, cfg.jitter, cfg.kind, cfg.nmodes, 2024))
+    dev = workload.DeviceCase(host, device=cuda)
+    m = learn.Mlp()
+    m.load(learn.SHIPPED_WEIGHTS)
+    import json
+
+    rep = json.load(open(os.path.join(os.path.dirname(learn.SHIPPED_WEIGHTS), "learned_48_report.json")))
+    r = learn.evaluate(m, dev, ybar=rep["ybar"], reps=1)
+    print("SHIPPED nu err %.3e const %.3e Rmom %.2e Rener %.2e fallback %.2e" % (
+        r["nu_rel_l2"], r["constant_ratio"]["nu_rel_l2"], r["Rmom_rel_l2"], r["Rener_rel_l2"], r["fallback_fraction"]))
+    assert r["nu_rel_l2"] < 0.4
+    assert r["nu_rel_l2"] < 0.5 * r["constant_ratio"]["nu_rel_l2"]
+    assert r["Rmom_rel_l2"] < 0.01 and r["Rener_rel_l2"] < 0.02
+    assert r["fallback_fraction"] < 0.01

@@ -77,3 +77,22 @@ def test_numpy_features_are_finite():
     assert np.all(np.isfinite(F)) and np.all(numax > 0)
     _, _, numax_o = O.entropy_viscosity(4, h.nelem, h.npoin, geom, f["rho"], f["u"], f["pr"])
     assert np.allclose(numax, numax_o, rtol=1e-12)
+
+
+def test_shipped_weight_file_format():
+    """The committed network: magic, sizes and CRC-32 of the weight file."""
+    import struct
+    import zlib
+
+    from minisod2d_gb300 import learn
+
+    b = open(learn.SHIPPED_WEIGHTS, "rb").read()
+    assert b[:8] == b"MSODMLP1"
+    ver, nin, nh, npar = struct.unpack("<4i", b[8:24])
+    assert (ver, nin, nh, npar) == (1, 12, 32, mlp_ref.NPARAMS)
+    assert len(b) == 24 + 4 * 48 + 2 * npar + 4
+    assert zlib.crc32(b[:-4]) == struct.unpack("<I", b[-4:])[0]
+    norm = np.frombuffer(b[24:24 + 192], np.float32)
+    assert np.all(norm[24:36] <= norm[36:48])  # training ranges
+    w = np.frombuffer(b[216:216 + 2 * npar], np.float16)
+    assert np.all(np.isfinite(w))
