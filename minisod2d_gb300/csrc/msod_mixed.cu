@@ -38,7 +38,7 @@
 // that direction and the point's own nodal values, to seven per-point
 // accumulators in shared memory; the last pass assembles the energy residual
 // in FP64 and scatter-adds all residuals with red.global.add.f64.
-// porder 1..7, one element per block of four warps.
+// porder 1..7; persistent blocks of four warps, one element at a time.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -155,6 +155,34 @@ __device__ __forceinline__ void mma_acc(float (&d)[4], const unsigned (&a)[4], u
                      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// float -> double by re-biasing the IEEE exponent on the integer pipe (FP64
+// arithmetic is scarce on this GPU); zeros, subnormals, infinities and NaNs
+// take the FP64 conversion.
+__device__ __forceinline__ double f2d(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const unsigned ex = (b >> 23) & 0xFFu;
+    if (ex == 0u || ex == 0xFFu) return (double)x;
+    const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
+                                    ((unsigned long long)(ex + (1023u - 127u)) << 52) |
+                                    ((unsigned long long)(b & 0x7FFFFFu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
+// Lattice point of slot s (s = 0, 1: line g of tile o1; 2, 3: line g of tile
+// o2; output point 2t + (s & 1) along direction d); -1 when padded.
+template <int Q>
+__device__ __forceinline__ int pass_point(int d, int s, int g, int tq, int o1, int o2, bool has1, bool has2)
+{
+    const int o = s < 2 ? o1 : o2;
+    const int pt = 2 * tq + (s & 1);
+    const int I = d == 0 ? pt : g;
+    const int J = d == 0 ? g : (d == 1 ? pt : o);
+    const int K = d == 2 ? pt : o;
+    const bool live = (s < 2 ? has1 : has2) && g < Q && pt < Q;
+    return live ? (K * Q + J) * Q + I : -1;
+}
+
 // Per-point coefficients of one direction pass.
 struct PointCoef {
     float rho, H, u[3], h[3], cu, cq;
@@ -231,15 +259,27 @@ __global__ void __launch_bounds__(kThreads)
     unsigned *sMax = reinterpret_cast<unsigned *>(sInv);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int e = blockIdx.x;
+    // Once per block: tables, the zero padding of the half planes (rows and
+    // points beyond Q are never written), the B fragments.
     for (int i = tid; i < N; i += kThreads) sPerm[i] = tabs->perm[i];
-    if (tid < 32) sMax[tid] = 0u;
-    if (Q < 8) {  // rows and points beyond Q stay zero
+    if (Q < 8) {
         uint4 *z = reinterpret_cast<uint4 *>(sHalf);
         for (int i = tid; i < (int)(G::half_bytes / 16); i += kThreads) z[i] = make_uint4(0, 0, 0, 0);
     }
-    __syncthreads();
+    // B fragments per direction: col lane/4 (output point), rows 2t, 2t+1 (input point).
+    unsigned Bh[3], Bl[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int r = lane >> 2, c0 = 2 * (lane & 3), c1 = c0 + 1;
+        const float d0 = (r < Q && c0 < Q) ? tabs->Df[(d * Q + r) * Q + c0] : 0.0f;
+        const float d1 = (r < Q && c1 < Q) ? tabs->Df[(d * Q + r) * Q + c1] : 0.0f;
+        split_pair<BF16>(d0, d1, Bh[d], Bl[d]);
+    }
     const size_t np = (size_t)npoin;
+#pragma unroll 1
+    for (int e = blockIdx.x; e < nelem; e += gridDim.x) {
+    __syncthreads();  // the previous element's passes are done with every shared array
+    if (tid < 32) sMax[tid] = 0u;
     for (int l = tid; l < N; l += kThreads) {
         const int a = sPerm[l];
         const int v = ldg(connec + (size_t)a * nelem + e) - 1;
@@ -256,6 +296,19 @@ __global__ void __launch_bounds__(kThreads)
         }
     }
     __syncthreads();
+
+    // He columns of the first direction pass, in flight during the split.
+    const int g = lane >> 2, tq = lane & 3;
+    const int o1 = warp, o2 = warp + 4 < Q ? warp + 4 : warp;
+    const bool has1 = o1 < Q, has2 = warp + 4 < Q;
+    float hcur[4][3];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int l = pass_point<Q>(0, s, g, tq, o1, o2, has1, has2);
+        const float *hp = He + ((size_t)e * N + sPerm[l < 0 ? 0 : l]) * 9;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) hcur[s][c] = ldg(hp + c);
+    }
 
     // Shifted products of the thread's tasks (two points each) in registers,
     // their per-field maxima over the element (non-negative floats order like
@@ -320,22 +373,9 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
 
-    // B fragments per direction: col g (output point), rows 2t, 2t+1 (input point).
-    const int g = lane >> 2, tq = lane & 3;
-    unsigned Bh[3], Bl[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const int c0 = 2 * tq, c1 = 2 * tq + 1;
-        const float d0 = (g < Q && c0 < Q) ? tabs->Df[(d * Q + g) * Q + c0] : 0.0f;
-        const float d1 = (g < Q && c1 < Q) ? tabs->Df[(d * Q + g) * Q + c1] : 0.0f;
-        split_pair<BF16>(d0, d1, Bh[d], Bl[d]);
-    }
-
     // Warp w takes the 16 lines of tiles o1 = w and o2 = w + 4 (k-planes for
     // xi / eta lines, j-planes for zeta lines); ldmatrix matrix m of the A
     // operand is (hi o1, hi o2, lo o1, lo o2), row r8.
-    const int o1 = warp, o2 = warp + 4 < Q ? warp + 4 : warp;
-    const bool has1 = o1 < Q, has2 = warp + 4 < Q;
     const int m = lane >> 3, r8 = lane & 7;
     const int om = (m & 1) ? o2 : o1;
     const int plane_off = (m >> 1) * kPlaneB;
@@ -348,30 +388,39 @@ __global__ void __launch_bounds__(kThreads)
         int lat[4];
         bool live[4];
         PointCoef cf[4];
-        float acc[4][NACC];
+        float acc[4][NACC], gp[4];
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-            const int o = s < 2 ? o1 : o2;
-            const int pt = 2 * tq + (s & 1);
-            const int I = d == 0 ? pt : g;
-            const int J = d == 0 ? g : (d == 1 ? pt : o);
-            const int K = d == 2 ? pt : o;
-            live[s] = (s < 2 ? has1 : has2) && g < Q && pt < Q;
-            const int l = live[s] ? (K * Q + J) * Q + I : 0;
+            const int lp = pass_point<Q>(d, s, g, tq, o1, o2, has1, has2);
+            live[s] = lp >= 0;
+            const int l = live[s] ? lp : 0;
             lat[s] = l;
             const Nodal n = nodal_from(sBase, N, l);
-            const float *hp = He + ((size_t)e * N + sPerm[l]) * 9 + d * 3;
             cf[s].rho = n.r;
             cf[s].H = n.H;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 cf[s].u[c] = n.u[c];
-                cf[s].h[c] = ldg(hp + c);
+                cf[s].h[c] = hcur[s][c];
             }
             cf[s].cu = n.u[0] * cf[s].h[0] + n.u[1] * cf[s].h[1] + n.u[2] * cf[s].h[2];
             cf[s].cq = n.q[0] * cf[s].h[0] + n.q[1] * cf[s].h[1] + n.q[2] * cf[s].h[2];
 #pragma unroll
             for (int k = 0; k < NACC; ++k) acc[s][k] = (d == 0 || !live[s]) ? 0.0f : sAcc[k * N + l];
+        }
+        // Loads in flight during the contractions: the next pass's He columns,
+        // or gpvol for the last pass's scatter.
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            if (d < 2) {
+                const int l = pass_point<Q>(d + 1, s, g, tq, o1, o2, has1, has2);
+                const float *hp = He + ((size_t)e * N + sPerm[l < 0 ? 0 : l]) * 9 + (d + 1) * 3;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) hcur[s][c] = ldg(hp + c);
+                gp[s] = 0.0f;
+            } else {
+                gp[s] = ldg(gpvol + (size_t)e * N + sPerm[lat[s]]);
+            }
         }
         const unsigned char *rowp =
             sHalf + plane_off + (d == 2 ? row_pos(r8, om) : row_pos(om, r8)) * kRowB;
@@ -403,22 +452,21 @@ __global__ void __launch_bounds__(kThreads)
                 const int node = sNode[lat[s]];
                 if (node < 0) continue;
                 const Nodal n = nodal_from(sBase, N, lat[s]);
-                const double gp = (double)ldg(gpvol + (size_t)e * N + sPerm[lat[s]]);
                 const float divU = acc[s][A_DIVU], divQ = acc[s][A_DIVQ];
                 const float rm = acc[s][A_M] + 0.5f * (divQ + n.r * divU);
-                // energy-flux assembly in FP64
-                const double re =
-                    (double)acc[s][A_E] + 0.25 * ((double)n.H * (double)divQ + (double)n.rH * (double)divU);
-                red_add(Rmass + node, gp * (double)rm);
-                red_add(Rener + node, gp * re);
+                red_add(Rmass + node, f2d(gp[s] * rm));
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
                     const float rmom = acc[s][A_MOM0 + i] + 0.25f * (n.u[i] * divQ + n.q[i] * divU);
-                    red_add(Rmom + (size_t)i * npoin + node, gp * (double)rmom);
+                    red_add(Rmom + (size_t)i * npoin + node, f2d(gp[s] * rmom));
                 }
+                // energy-flux assembly in FP64
+                const double t = fma(f2d(n.H), f2d(divQ), f2d(n.rH) * f2d(divU));
+                red_add(Rener + node, f2d(gp[s]) * fma(0.25, t, f2d(acc[s][A_E])));
             }
         }
     }
+    }  // elements
 }
 
 template <int P, bool BF16>
@@ -430,7 +478,9 @@ cudaError_t launch_mixed_pb(const MixedConvecArgs &a, const TableScratch *tabs, 
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem);
     if (err != cudaSuccess) return err;
     if (a.nelem == 0) return cudaSuccess;
-    kern<<<a.nelem, kThreads, G::smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, tabs, a.u, a.q, a.rho,
+    const int grid = persistent_grid(kern, kThreads, G::smem, a.nelem);
+    if (grid < 1) return cudaErrorInvalidConfiguration;
+    kern<<<grid, kThreads, G::smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, tabs, a.u, a.q, a.rho,
                                              a.pr, a.E, a.Rmass, a.Rmom, a.Rener);
     return cudaGetLastError();
 }
