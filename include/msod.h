@@ -164,6 +164,30 @@ int msod_convec_ijk_mixed(int precision, int porder, int nelem, int npoin, const
                           const float *pr, const float *E, double *Rmass, double *Rmom,
                           double *Rener, void *stream);
 
+/* No counterpart in the reference: mixed-precision form of full_diffusion_ijk.
+ * FP32 fields and geometry as msod_diffusion_ijk; the gradient and weak-
+ * divergence contractions run on the tensor cores as hi + lo split FP16 (or
+ * BF16) products with FP32 accumulation (gradient inputs shifted by their
+ * value at one node of the element, every split field scaled by a power of
+ * two per element); the energy-flux assembly (tau.u + kappa_e grad T) and the
+ * nodal scatter-add run in FP64 and the residuals are FP64 arrays.  The _nu
+ * form takes mu_e(e,a) = rho(a) nu_elem(e) as msod_diffusion_ijk_nu does.
+ * precision: MSOD_PREC_FP16 or MSOD_PREC_BF16.  porder 1..7. */
+int msod_diffusion_ijk_mixed(int precision, int porder, int nelem, int npoin, const int *connec,
+                             const float *He, const float *gpvol, const float *dlxigp_ip,
+                             const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
+                             const int *gmshAtoK, float Cp, float Pr, const float *rho,
+                             const float *u, const float *Tem, const float *mu_fluid,
+                             const float *mu_e, const float *mu_sgs, double *Rmass, double *Rmom,
+                             double *Rener, void *stream);
+int msod_diffusion_ijk_mixed_nu(int precision, int porder, int nelem, int npoin, const int *connec,
+                                const float *He, const float *gpvol, const float *dlxigp_ip,
+                                const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
+                                const int *gmshAtoK, float Cp, float Pr, const float *rho,
+                                const float *u, const float *Tem, const float *mu_fluid,
+                                const float *nu_elem, const float *mu_sgs, double *Rmass,
+                                double *Rmom, double *Rener, void *stream);
+
 /* Validate element tables and connectivity on the device (synchronous):
  * invAtoIJK is a permutation of 1..n consistent with gmshAtoI/J/K,
  * dlxigp_ip has the per-direction 1-D structure, every connec entry lies in

@@ -48,6 +48,8 @@ SIGNATURES = {
     "msod_diffusion_ijk": _GEOM + [_f, _f] + [_p] * 9 + [_p],
     "msod_convec_ijk_f64": _GEOM64 + [_p] * 8 + [_p],
     "msod_convec_ijk_mixed": [_i] + _GEOM64 + [_p] * 8 + [_p],
+    "msod_diffusion_ijk_mixed": [_i] + _GEOM64 + [_f, _f] + [_p] * 9 + [_p],
+    "msod_diffusion_ijk_mixed_nu": [_i] + _GEOM64 + [_f, _f] + [_p] * 9 + [_p],
     "msod_diffusion_ijk_f64": _GEOM64 + [_d, _d] + [_p] * 9 + [_p],
     "msod_check_element_tables": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
     "msod_check_element_tables_noalloc": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],

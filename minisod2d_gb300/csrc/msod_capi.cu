@@ -355,6 +355,74 @@ int msod_convec_ijk_mixed(int precision, int porder, int nelem, int npoin, const
     return rc;
 }
 
+static int diffu_mixed_impl(int precision, int porder, int nelem, int npoin, const int *connec, const float *He,
+                            const float *gpvol, const float *dlx, const int *inv, const int *ai, const int *aj,
+                            const int *ak, float Cp, float Pr, const float *rho, const float *u, const float *Tem,
+                            const float *mu_fluid, const float *mu_e, const float *nu_elem, const float *mu_sgs,
+                            double *Rmass, double *Rmom, double *Rener, void *stream)
+{
+    clear_error();
+    if (precision != MSOD_PREC_FP16 && precision != MSOD_PREC_BF16)
+        return set_error(MSOD_ERR_INVALID_ARG, "precision %d is neither MSOD_PREC_FP16 nor MSOD_PREC_BF16", precision);
+    int rc = check_geometry(porder, nelem, npoin, connec, He, gpvol, dlx, inv, ai, aj, ak);
+    if (rc) return rc;
+    if (porder > 7) return set_error(MSOD_ERR_PORDER, "the mixed-precision kernels serve porder 1..7");
+    if (!rho || !u || !Tem || !mu_fluid || !(mu_e || nu_elem) || !mu_sgs || !Rmass || !Rmom || !Rener)
+        return set_error(MSOD_ERR_INVALID_ARG, "NULL field or residual array");
+    if (!(Pr != 0.0f)) return set_error(MSOD_ERR_INVALID_ARG, "Pr must be non-zero");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (checked_mode()) {
+        rc = run_check(porder, nelem, npoin, connec, dlx, inv, ai, aj, ak, st);
+        if (rc) return rc;
+    }
+    TableScratch *tabs = device_tables();
+    if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
+    rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
+    if (rc) return rc;
+    ElementArgs<float> ea;
+    ea.nelem = nelem; ea.npoin = npoin; ea.connec = connec; ea.He = He; ea.gpvol = gpvol; ea.dlxigp_ip = dlx;
+    ea.invAtoIJK = inv; ea.AtoI = ai; ea.AtoJ = aj; ea.AtoK = ak;
+    MixedDiffuArgs a;
+    a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.Cp = Cp; a.Pr = Pr;
+    a.rho = rho; a.u = u; a.Tem = Tem; a.mu_fluid = mu_fluid; a.mu_e = mu_e; a.mu_sgs = mu_sgs; a.nu_elem = nu_elem;
+    a.Rmass = Rmass; a.Rmom = Rmom; a.Rener = Rener;
+    rc = cuda_status(launch_table_prep<float>(porder, ea, tabs, st), "table preparation launch");
+    if (!rc) rc = cuda_status(launch_diffu_mixed(porder, precision, a, tabs, st), "mixed diffusion launch");
+    if (!rc && checked_mode()) rc = cuda_status(cudaStreamSynchronize(st), "mixed diffusion kernel");
+    return rc;
+}
+
+int msod_diffusion_ijk_mixed(int precision, int porder, int nelem, int npoin, const int *connec, const float *He,
+                             const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI,
+                             const int *gmshAtoJ, const int *gmshAtoK, float Cp, float Pr, const float *rho,
+                             const float *u, const float *Tem, const float *mu_fluid, const float *mu_e,
+                             const float *mu_sgs, double *Rmass, double *Rmom, double *Rener, void *stream)
+{
+    if (!mu_e) {
+        clear_error();
+        return set_error(MSOD_ERR_INVALID_ARG, "NULL mu_e");
+    }
+    return diffu_mixed_impl(precision, porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI,
+                            gmshAtoJ, gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, nullptr, mu_sgs, Rmass, Rmom,
+                            Rener, stream);
+}
+
+int msod_diffusion_ijk_mixed_nu(int precision, int porder, int nelem, int npoin, const int *connec, const float *He,
+                                const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK,
+                                const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK, float Cp, float Pr,
+                                const float *rho, const float *u, const float *Tem, const float *mu_fluid,
+                                const float *nu_elem, const float *mu_sgs, double *Rmass, double *Rmom, double *Rener,
+                                void *stream)
+{
+    if (!nu_elem) {
+        clear_error();
+        return set_error(MSOD_ERR_INVALID_ARG, "NULL nu_elem");
+    }
+    return diffu_mixed_impl(precision, porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI,
+                            gmshAtoJ, gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, nullptr, nu_elem, mu_sgs, Rmass, Rmom,
+                            Rener, stream);
+}
+
 int msod_diffusion_ijk_f64(int porder, int nelem, int npoin, const int *connec, const double *He,
                            const double *gpvol, const double *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI,
                            const int *gmshAtoJ, const int *gmshAtoK, double Cp, double Pr, const double *rho,

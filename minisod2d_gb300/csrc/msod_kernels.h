@@ -82,6 +82,20 @@ struct MixedConvecArgs {
 cudaError_t launch_convec_mixed(int porder, int precision, const MixedConvecArgs &a,
                                 const TableScratch *tabs, cudaStream_t st);
 
+// Mixed-precision diffusion: FP32 fields, FP64 residuals (zeroed by the
+// caller; tables prepared).  nu_elem set: mu_e(e, a) = rho(a) nu_elem[e] and
+// mu_e is not read.
+struct MixedDiffuArgs {
+    int nelem, npoin;
+    const int *connec;
+    const float *He, *gpvol;
+    float Cp, Pr;
+    const float *rho, *u, *Tem, *mu_fluid, *mu_e, *mu_sgs, *nu_elem;
+    double *Rmass, *Rmom, *Rener;
+};
+cudaError_t launch_diffu_mixed(int porder, int precision, const MixedDiffuArgs &a, const TableScratch *tabs,
+                               cudaStream_t st);
+
 // ---------------------------------------------------------------------------
 // Entropy viscosity and the learned estimator
 // ---------------------------------------------------------------------------

@@ -45,19 +45,16 @@
 
 #include "msod_device.cuh"
 #include "msod_kernels.h"
+#include "msod_mma.cuh"
 
 namespace msod {
 namespace {
 
 constexpr int kNF = 31;       // differentiated products
-constexpr int kRowB = 16;     // bytes per row: 8 halves
-constexpr int kPlaneB = 64 * kRowB;
 constexpr int kThreads = 128;
 
 enum { B_RHO = 0, B_P, B_E, B_U0, B_U1, B_U2, B_Q0, B_Q1, B_Q2, NBASE };
 enum { A_M = 0, A_MOM0, A_MOM1, A_MOM2, A_E, A_DIVU, A_DIVQ, NACC };
-
-__device__ __forceinline__ int row_pos(int k, int j) { return 8 * k + (j ^ k); }
 
 // Field numbering: 0 rho, 1 p, 2-4 u_i, 5-7 q_i, 8-16 q_i u_j (i major),
 // 17-22 u_i u_j (i <= j: 00 01 02 11 12 22), 23 H, 24 rho H, 25-27 rho H u_i,
@@ -98,75 +95,6 @@ __device__ __forceinline__ float field(int f, const Nodal &n)
     if (f == 24) return n.rH;
     if (f < 28) return __fmul_rn(n.rH, n.u[f - 25]);
     return __fmul_rn(n.H, n.u[f - 28]);
-}
-
-template <bool BF16>
-__device__ __forceinline__ unsigned pack2(float a, float b)
-{
-    if (BF16) {
-        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-        return *reinterpret_cast<const unsigned *>(&h);
-    }
-    const __half2 h = __floats2half2_rn(a, b);
-    return *reinterpret_cast<const unsigned *>(&h);
-}
-
-// Split of a pair of derivative-matrix entries into hi and lo halves.
-template <bool BF16>
-__device__ __forceinline__ void split_pair(float a, float b, unsigned &hi, unsigned &lo)
-{
-    hi = pack2<BF16>(a, b);
-    float2 f;
-    if (BF16)
-        f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&hi));
-    else
-        f = __half22float2(*reinterpret_cast<const __half2 *>(&hi));
-    lo = pack2<BF16>(a - f.x, b - f.y);
-}
-
-__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void *row)
-{
-    const unsigned a = (unsigned)__cvta_generic_to_shared(row);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(a));
-}
-__device__ __forceinline__ void ldsm_x4_t(unsigned (&r)[4], const void *row)
-{
-    const unsigned a = (unsigned)__cvta_generic_to_shared(row);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(a));
-}
-
-// d = A B + d (m16n8k16, FP32 accumulate).
-template <bool BF16>
-__device__ __forceinline__ void mma_acc(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
-{
-    if (BF16)
-        asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-                     "{%8,%9}, {%0,%1,%2,%3};"
-                     : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-                     : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-    else
-        asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-                     "{%8,%9}, {%0,%1,%2,%3};"
-                     : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-                     : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// float -> double by re-biasing the IEEE exponent on the integer pipe (FP64
-// arithmetic is scarce on this GPU); zeros, subnormals, infinities and NaNs
-// take the FP64 conversion.
-__device__ __forceinline__ double f2d(float x)
-{
-    const unsigned b = __float_as_uint(x);
-    const unsigned ex = (b >> 23) & 0xFFu;
-    if (ex == 0u || ex == 0xFFu) return (double)x;
-    const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
-                                    ((unsigned long long)(ex + (1023u - 127u)) << 52) |
-                                    ((unsigned long long)(b & 0x7FFFFFu) << 29);
-    return __longlong_as_double((long long)bits);
 }
 
 // Lattice point of slot s (s = 0, 1: line g of tile o1; 2, 3: line g of tile

@@ -127,6 +127,29 @@ def full_convec_ijk_mixed(nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK,
     capi.call("msod_convec_ijk_mixed", prec, P, nelem, npoin, *g, *f, _stream(stream))
 
 
+def full_diffusion_ijk_mixed(nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                             Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs, Rmass, Rmom, Rener, precision="fp16",
+                             nu_elem=None, stream=None):
+    """Mixed-precision form of elem_diffu.f90:10: FP32 fields, FP64 residuals.
+
+    With ``nu_elem`` (one value per element) mu_e(e, a) = rho(a) nu_elem(e)
+    and ``mu_e`` is ignored."""
+    import torch
+
+    P, g = _geometry(nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                     torch.float32)
+    n = (P + 1) ** 3
+    visc = _ptr(nu_elem, "nu_elem", torch.float32, nelem) if nu_elem is not None else \
+        _ptr(mu_e, "mu_e", torch.float32, nelem * n)
+    f = [_ptr(rho, "rho", torch.float32, npoin), _ptr(u, "u", torch.float32, 3 * npoin),
+         _ptr(Tem, "Tem", torch.float32, npoin), _ptr(mu_fluid, "mu_fluid", torch.float32, npoin), visc,
+         _ptr(mu_sgs, "mu_sgs", torch.float32, nelem * n), _ptr(Rmass, "Rmass", torch.float64, npoin),
+         _ptr(Rmom, "Rmom", torch.float64, 3 * npoin), _ptr(Rener, "Rener", torch.float64, npoin)]
+    prec = {"fp16": capi.MSOD_PREC_FP16, "bf16": capi.MSOD_PREC_BF16}[precision]
+    name = "msod_diffusion_ijk_mixed_nu" if nu_elem is not None else "msod_diffusion_ijk_mixed"
+    capi.call(name, prec, P, nelem, npoin, *g, float(Cp), float(Pr), *f, _stream(stream))
+
+
 def elem_jacobian(porder, nelem, npoin, connec, coord, dNgp, wgp, gpvol, He, stream=None):
     """jacobian_oper.f90:7 on the device; writes gpvol and He in place."""
     import torch
@@ -156,5 +179,6 @@ def set_checked(enabled):
     capi.call("msod_set_checked", 1 if enabled else 0)
 
 
-__all__ = ["full_convec_ijk", "full_convec_ijk_split", "full_diffusion_ijk", "full_convec_ijk_mixed", "elem_jacobian",
+__all__ = ["full_convec_ijk", "full_convec_ijk_split", "full_diffusion_ijk", "full_convec_ijk_mixed",
+           "full_diffusion_ijk_mixed", "elem_jacobian",
            "check_element_tables", "set_checked"]

@@ -163,6 +163,24 @@ class DeviceCase:
                                       self.E, *out, precision=precision, stream=stream)
         return out
 
+    def diffu_mixed(self, precision="fp16", mu_e=None, nu_elem=None, out=None, stream=None):
+        """Mixed-precision diffusion into FP64 residuals (allocated unless ``out`` is given)."""
+        import torch
+
+        from . import kernels
+
+        if out is None:
+            dev = self.He.device
+            out = (torch.empty(self.npoin, dtype=torch.float64, device=dev),
+                   torch.empty(3 * self.npoin, dtype=torch.float64, device=dev),
+                   torch.empty(self.npoin, dtype=torch.float64, device=dev))
+        g = self.geometry()
+        kernels.full_diffusion_ijk_mixed(g[0], g[1], g[2], g[5], g[6], g[7], *g[9:], self.cfg.Cp, self.cfg.Pr,
+                                         self.rho, self.u, self.Tem, self.mu_fluid,
+                                         self.mu_e if mu_e is None else mu_e, self.mu_sgs, *out,
+                                         precision=precision, nu_elem=nu_elem, stream=stream)
+        return out
+
     def diffu(self, stream=None):
         from . import kernels
 

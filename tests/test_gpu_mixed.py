@@ -2,11 +2,15 @@
 contractions, FP64 scatter and energy-flux assembly).
 
 Reference: the FP64 oracle on the same inputs (the FP32 fields and geometry
-the kernel reads, promoted to FP64).  Criterion per residual: relative L2
-<= 1e-4 for both formats, and <= 1e-5 for FP16 (whose split carries about 22
-bits of each product's variation over the element).  The plain FP32 GPU
-kernel's distance from the same FP64 answer (the FP32 floor) is printed
-beside it.
+the kernel reads, promoted to FP64).  The plain FP32 GPU kernel's distance
+from the same FP64 answer (the FP32 floor) is printed beside each result.
+Criteria per residual (relative L2):
+  * convection: <= 1e-4 for both formats and <= 1e-5 for FP16;
+  * diffusion: <= max(1e-4, 6 x floor) for FP16 and <= max(2e-4, 6 x floor)
+    for BF16.  Its weak divergence cancels strongly between neighbouring
+    elements (the FP32 floor itself reaches 4e-4 for the energy residual of
+    the 32^3 porder-7 workload), and the tensor-core contractions land at
+    4-7 x that floor.
 """
 import numpy as np
 import pytest
@@ -19,6 +23,7 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-4
 TOL_FP16 = 1e-5
+DIFFU_FLOOR_FACTOR = 6.0
 
 
 def _case(cuda, P, nx, kind=0, nmodes=8, seed=0, jitter=0.05):
@@ -96,3 +101,52 @@ def test_mixed_rejects_bad_arguments(cuda):
         capi.call("msod_convec_ijk_mixed", 5, 4, dev.nelem, dev.npoin, *[t.data_ptr() for t in args[2:]],
                   *[t.data_ptr() for t in out], torch.cuda.current_stream().cuda_stream)
     assert ei.value.code == capi.MSOD_ERR_INVALID_ARG
+
+
+def _diffu_case(cuda, P, nx, kind, nmodes, mu=1e-3, seed=0):
+    cfg = workload.Config("t", P, nx, 0.05, kind, nmodes, seed)
+    host = workload.HostCase(cfg)
+    rng = np.random.default_rng(seed + 11)
+    host.mu_e = (mu * rng.random(host.mu_e.size)).astype(np.float32)
+    host.mu_sgs = (0.5 * mu * rng.random(host.mu_sgs.size)).astype(np.float32)
+    return host, workload.DeviceCase(host, device=cuda)
+
+
+def _diffu_oracle64(host, dev, mu_e=None):
+    t = host.tables
+    geom = dict(t, connec=host.connec, He=dev.He.cpu().numpy(), gpvol=dev.gpvol.cpu().numpy())
+    f = host.fields
+    return O.full_diffusion_ijk(dev.cfg.porder, dev.nelem, dev.npoin, geom, dev.cfg.Cp, dev.cfg.Pr, f["rho"], f["u"],
+                                f["Tem"], f["mu_fluid"], host.mu_e if mu_e is None else mu_e, host.mu_sgs,
+                                dtype=np.float64, nthreads=8)
+
+
+@pytest.mark.parametrize("P,nx,kind,nmodes", [(7, 3, 0, 16), (5, 4, 1, 8), (4, 4, 0, 8), (2, 5, 1, 8)])
+def test_mixed_diffusion_vs_fp64_oracle(cuda, P, nx, kind, nmodes):
+    host, dev = _diffu_case(cuda, P, nx, kind, nmodes)
+    ref = _diffu_oracle64(host, dev)
+    floor = _errs(dev.diffu(), ref)
+    for prec in ("fp16", "bf16"):
+        errs = _errs(dev.diffu_mixed(prec), ref)
+        print("MIXED-DIFFU P=%d kind=%d %s err=%s floor32=%s" % (
+            P, kind, prec, ["%.2e" % x for x in errs], ["%.2e" % x for x in floor]))
+        # The weak divergence cancels strongly between neighbouring elements,
+        # so the diffusion bound is stated against the FP32 floor.
+        for name, e, fl in zip(("mass", "mom", "ener"), errs, floor):
+            bound = max(TOL if prec == "fp16" else 2 * TOL, DIFFU_FLOOR_FACTOR * fl)
+            assert e <= bound, (prec, name, e, fl)
+
+
+def test_mixed_diffusion_per_element_viscosity(cuda):
+    """The _nu form equals the mu_e-array form with mu_e(e, a) = rho(a) nu(e)."""
+    import torch
+
+    host, dev = _diffu_case(cuda, 5, 3, 1, 8)
+    nu = torch.rand(dev.nelem, device=cuda) * 1e-3
+    n = dev.cfg.nnode
+    node = dev.connec.view(n, dev.nelem).long() - 1
+    mu_arr = (dev.rho[node] * nu.view(1, -1)).reshape(-1).contiguous()
+    a = dev.diffu_mixed("fp16", nu_elem=nu)
+    b = dev.diffu_mixed("fp16", mu_e=mu_arr)
+    for x, y in zip(a, b):
+        assert refimpl.rel_l2(x.cpu().numpy(), y.cpu().numpy()) < 1e-6
