@@ -14,6 +14,12 @@ energy) for the full right-hand side.  Inputs (2.4 GB per call) exceed the
 
 Under torchrun each rank runs its own replica of the workload (weak scaling,
 no collective on the data path); rank 0 prints the max-over-ranks timing.
+
+On one GPU the line also carries "variants": the mixed-precision kernels on
+the 32^3 porder-7 workload, the learned viscosity on a held-out seed of the
+48^3 shock workload and the combined 96^3 porder-5 workload, each timed with
+CUDA events beside the plain kernels, with errors against the FP64 build of
+the plain kernels (--no-variants skips them).
 """
 import argparse
 import json
@@ -62,11 +68,16 @@ class ClockSampler:
         self.file = None
 
     def start(self):
+        """Start sampling every 50 ms; returns once the first sample is in, so
+        that the samples that follow fall inside the timed region."""
         try:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.file,
                                          stderr=subprocess.DEVNULL)
+            t0 = time.time()
+            while time.time() - t0 < 5.0 and os.path.getsize(self.file.name) == 0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
 
@@ -172,18 +183,26 @@ def cpu_step(cfg, host, geom, ne, mu, nthreads):
 
 
 def calibrate_sample(cfg, host, nthreads, seconds):
-    """Number of elements whose convec+diffu takes about `seconds` on `nthreads`."""
-    ne = 256 if nthreads == 1 else 256 * nthreads
+    """Number of elements whose convec+diffu takes about `seconds` on `nthreads`
+    (a warm-up call first, then a timed probe of about a tenth of the target)."""
+    ne = 64 * nthreads
     geom, ne, mu = cpu_sample_case(cfg, host, ne)
-    t0 = time.perf_counter()
     cpu_step(cfg, host, geom, ne, mu, nthreads)
-    dt = max(time.perf_counter() - t0, 1e-3)
+    for _ in range(2):
+        t0 = time.perf_counter()
+        cpu_step(cfg, host, geom, ne, mu, nthreads)
+        dt = max(time.perf_counter() - t0, 1e-4)
+        if dt > 0.05 * seconds or ne >= host.nelem:
+            break
+        ne = min(host.nelem, int(ne * 0.1 * seconds / dt) + 1)
+        geom, ne, mu = cpu_sample_case(cfg, host, ne)
     want = int(ne * seconds / dt)
     return max(64, min(host.nelem, want))
 
 
-def cpu_baseline(cfg, host, seconds=12.0):
-    """The serial oracle (the faithful single-core restatement) on a bounded sample."""
+def cpu_baseline(cfg, host, seconds=15.0):
+    """The serial oracle (the faithful single-core restatement) on a bounded sample
+    of about `seconds` of CPU work."""
     ns = calibrate_sample(cfg, host, 1, seconds)
     geom, ne, mu = cpu_sample_case(cfg, host, ns)
     t0 = time.perf_counter()
@@ -371,25 +390,192 @@ def run_ours(args, cfg, rank, local, world):
         "kernels": {"convec_ms": conv_ms, "diffu_ms": diff_ms, "convec_gbs": Bc / conv_ms / 1e6,
                     "diffu_gbs": Bd / diff_ms / 1e6,
                     "combined_frac": (Bc + Bd) / ((conv_ms + diff_ms) * 1e-3) / 1e9 / peak},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 3 * args.steps,  # per step: convection kernel, table preparation, diffusion kernel
         "clocks": clocks,
         "e2e": e2e,
     }
     if world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(cfg, host, args.cpu_seconds)
+    if world == 1 and not args.no_variants:
+        del dev
+        out["variants"] = run_variants()
     print(json.dumps(out))
+
+
+# --------------------------------------------------------------------------------------
+# Variants beside the plain step: mixed precision and the learned viscosity
+# --------------------------------------------------------------------------------------
+def _ms(fn, reps):
+    import torch
+
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    b.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def _rel(a, b):
+    import torch
+
+    nb = float(torch.linalg.vector_norm(b.double()))
+    d = float(torch.linalg.vector_norm((a.double() - b.double())))
+    return d / nb if nb > 0 else d
+
+
+def _fp64_runs(dev, mu_e=None):
+    """The plain kernels' FP64 build on the FP32 inputs promoted to FP64 (the GPU FP64 oracle run)."""
+    import torch
+
+    from minisod2d_gb300 import kernels
+
+    g = dev.geometry()
+    d = lambda t: t.double()
+    mk = lambda: (torch.empty(dev.npoin, dtype=torch.float64, device=dev.He.device),
+                  torch.empty(3 * dev.npoin, dtype=torch.float64, device=dev.He.device),
+                  torch.empty(dev.npoin, dtype=torch.float64, device=dev.He.device))
+    geo = (g[0], g[1], g[2], None, None, d(dev.He), d(dev.gpvol), d(dev.dlxigp_ip), None, *g[9:])
+    c64, d64 = mk(), mk()
+    kernels.full_convec_ijk(*geo, d(dev.u), d(dev.q), d(dev.rho), d(dev.pr), d(dev.E), *c64)
+    kernels.full_diffusion_ijk(*geo, dev.cfg.Cp, dev.cfg.Pr, d(dev.rho), d(dev.u), d(dev.Tem), d(dev.mu_fluid),
+                               d(dev.mu_e if mu_e is None else mu_e), d(dev.mu_sgs), *d64)
+    torch.cuda.synchronize()
+    return c64, d64
+
+
+def variant_mixed(reps):
+    """mixed_p7: plain FP32 kernels against the FP16 / BF16 tensor-core kernels."""
+    import torch
+
+    from minisod2d_gb300 import workload
+
+    cfg = workload.CONFIGS["mixed_p7"]
+    dev = workload.DeviceCase(workload.HostCase(cfg))
+    c64, d64 = _fp64_runs(dev)
+    names = ("Rmass", "Rmom", "Rener")
+    res = {"workload": "mixed_p7: 32^3 hexes, porder 7, +-5% jitter, 16-mode smooth fields",
+           "error_reference": "FP64 build of the plain kernels on the same inputs"}
+    pc, pd = _ms(lambda: dev.convec(), reps), _ms(lambda: dev.diffu(), reps)
+    c32, d32 = dev.convec(), dev.diffu()
+    res["plain_fp32"] = {"convec_ms": pc, "diffu_ms": pd,
+                         "convec_err": {k: _rel(a, b) for k, a, b in zip(names, c32, c64)},
+                         "diffu_err": {k: _rel(a, b) for k, a, b in zip(names, d32, d64)}}
+    out = tuple(torch.empty_like(x) for x in c64)
+    for prec in ("fp16", "bf16"):
+        mc = _ms(lambda: dev.convec_mixed(prec, out=out), reps)
+        ce = {k: _rel(a, b) for k, a, b in zip(names, dev.convec_mixed(prec, out=out), c64)}
+        md = _ms(lambda: dev.diffu_mixed(prec, out=out), reps)
+        de = {k: _rel(a, b) for k, a, b in zip(names, dev.diffu_mixed(prec, out=out), d64)}
+        res[prec] = {"convec_ms": mc, "diffu_ms": md, "convec_err": ce, "diffu_err": de,
+                     "speedup_vs_plain": (pc + pd) / (mc + md)}
+    return res
+
+
+def variant_learned(reps):
+    """learned_48 on a held-out seed: the shipped network against the plain estimator."""
+    from minisod2d_gb300 import learn, workload
+
+    cfg = workload.CONFIGS["learned_48"]
+    host = workload.HostCase(workload.Config(cfg.name, cfg.porder, cfg.nx, cfg.jitter, cfg.kind, cfg.nmodes, 2024))
+    dev = workload.DeviceCase(host)
+    m = learn.Mlp()
+    m.load(learn.SHIPPED_WEIGHTS)
+    with open(os.path.join(os.path.dirname(learn.SHIPPED_WEIGHTS), "learned_48_report.json")) as f:
+        ybar = json.load(f)["ybar"]
+    r = learn.evaluate(m, dev, ybar=ybar, reps=reps)
+    r["workload"] = "learned_48: 48^3 hexes, porder 4, shock-like fields, held-out seed 2024"
+    r["speedup_estimator_plus_diffusion"] = r["ms_plain_estimator_plus_diffusion"] / \
+        r["ms_learned_estimator_plus_diffusion"]
+    return r
+
+
+def variant_combined(reps):
+    """combined_96: plain path (convection, entropy estimator, diffusion) against the
+    learned path and the mixed + learned path."""
+    import torch
+
+    from minisod2d_gb300 import learn, workload
+
+    cfg = workload.CONFIGS["combined_96"]
+    dev = workload.DeviceCase(workload.HostCase(cfg))
+    m = learn.Mlp()
+    m.load(learn.SHIPPED_WEIGHTS)
+    names = ("Rmass", "Rmom", "Rener")
+    mu_p, nu_p, numax = learn.entropy_viscosity(dev)
+    c64, d64 = _fp64_runs(dev, mu_e=mu_p)
+    nu_l, flag = learn.learned_viscosity(m, dev)
+    o64 = tuple(torch.empty_like(x) for x in c64)
+    o64b = tuple(torch.empty_like(x) for x in c64)
+    mu_buf = torch.empty_like(mu_p)
+
+    def plain():
+        dev.convec()
+        learn.entropy_viscosity(dev, mu_buf, nu_p, numax)
+        from minisod2d_gb300 import kernels
+        kernels.full_diffusion_ijk(*dev.geometry(), cfg.Cp, cfg.Pr, dev.rho, dev.u, dev.Tem, dev.mu_fluid, mu_buf,
+                                   dev.mu_sgs, dev.Dmass, dev.Dmom, dev.Dener)
+
+    def learned32():
+        dev.convec()
+        learn.learned_viscosity(m, dev, nu_l, flag)
+        learn.diffusion_ijk_nu(dev, nu_l)
+
+    def mixed_learned():
+        dev.convec_mixed("fp16", out=o64)
+        learn.learned_viscosity(m, dev, nu_l, flag)
+        dev.diffu_mixed("fp16", nu_elem=nu_l, out=o64b)
+
+    t_plain, t_l32, t_ml = _ms(plain, reps), _ms(learned32, reps), _ms(mixed_learned, reps)
+    plain()
+    pe = {"convec": {k: _rel(a, b) for k, a, b in zip(names, (dev.Rmass, dev.Rmom, dev.Rener), c64)},
+          "diffu": {k: _rel(a, b) for k, a, b in zip(names, (dev.Dmass, dev.Dmom, dev.Dener), d64)}}
+    learned32()
+    le = {"diffu": {k: _rel(a, b) for k, a, b in zip(names, (dev.Dmass, dev.Dmom, dev.Dener), d64)}}
+    mixed_learned()
+    me = {"convec": {k: _rel(a, b) for k, a, b in zip(names, o64, c64)},
+          "diffu": {k: _rel(a, b) for k, a, b in zip(names, o64b, d64)}}
+    dofs = 5.0 * dev.npoin
+    return {"workload": "combined_96: 96^3 hexes, porder 5, +-5% jitter, shock-like fields",
+            "error_reference": "FP64 build of the plain kernels on the same inputs, diffusion with the plain "
+                               "estimator's mu_e",
+            "plain": {"ms": t_plain, "gdofs": dofs / t_plain / 1e6, "err": pe},
+            "learned_fp32": {"ms": t_l32, "gdofs": dofs / t_l32 / 1e6, "err": le, "speedup": t_plain / t_l32},
+            "mixed_fp16_learned": {"ms": t_ml, "gdofs": dofs / t_ml / 1e6, "err": me, "speedup": t_plain / t_ml},
+            "fallback_fraction": float(flag.float().mean()),
+            "nu_rel_l2_learned_vs_plain": _rel(nu_l, nu_p)}
+
+
+def run_variants(reps=10):
+    out = {}
+    for name, fn in (("mixed_p7", variant_mixed), ("learned_48", variant_learned),
+                     ("combined_96", variant_combined)):
+        import torch
+
+        try:
+            out[name] = fn(reps)
+        except Exception as ex:  # a variant never costs the plain measurement
+            out[name] = {"error": "%s: %s" % (type(ex).__name__, ex)}
+        torch.cuda.empty_cache()
+    return out
 
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="plain_64")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the mixed-precision / learned-viscosity measurements beside the plain step")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # the timing rules ask for at least 3 warm-up steps
     from minisod2d_gb300 import workload
