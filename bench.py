@@ -484,10 +484,8 @@ def variant_learned(reps):
     host = workload.HostCase(workload.Config(cfg.name, cfg.porder, cfg.nx, cfg.jitter, cfg.kind, cfg.nmodes, 2024))
     dev = workload.DeviceCase(host)
     m = learn.Mlp()
-    m.load(learn.SHIPPED_WEIGHTS)
-    with open(os.path.join(os.path.dirname(learn.SHIPPED_WEIGHTS), "learned_48_report.json")) as f:
-        ybar = json.load(f)["ybar"]
-    r = learn.evaluate(m, dev, ybar=ybar, reps=reps)
+    m.load(learn.shipped_weights("learned_48"))
+    r = learn.evaluate(m, dev, ybar=learn.shipped_report("learned_48")["ybar"], reps=reps)
     r["workload"] = "learned_48: 48^3 hexes, porder 4, shock-like fields, held-out seed 2024"
     r["speedup_estimator_plus_diffusion"] = r["ms_plain_estimator_plus_diffusion"] / \
         r["ms_learned_estimator_plus_diffusion"]
@@ -502,9 +500,10 @@ def variant_combined(reps):
     from minisod2d_gb300 import learn, workload
 
     cfg = workload.CONFIGS["combined_96"]
-    dev = workload.DeviceCase(workload.HostCase(cfg))
+    dev = workload.DeviceCase(workload.HostCase(
+        workload.Config(cfg.name, cfg.porder, cfg.nx, cfg.jitter, cfg.kind, cfg.nmodes, 2024)))  # held-out seed
     m = learn.Mlp()
-    m.load(learn.SHIPPED_WEIGHTS)
+    m.load(learn.shipped_weights("combined_96"))
     names = ("Rmass", "Rmom", "Rener")
     mu_p, nu_p, numax = learn.entropy_viscosity(dev)
     c64, d64 = _fp64_runs(dev, mu_e=mu_p)
@@ -540,7 +539,8 @@ def variant_combined(reps):
     me = {"convec": {k: _rel(a, b) for k, a, b in zip(names, o64, c64)},
           "diffu": {k: _rel(a, b) for k, a, b in zip(names, o64b, d64)}}
     dofs = 5.0 * dev.npoin
-    return {"workload": "combined_96: 96^3 hexes, porder 5, +-5% jitter, shock-like fields",
+    return {"workload": "combined_96: 96^3 hexes, porder 5, +-5% jitter, shock-like fields, held-out seed 2024; "
+                        "network trained on 16 other seeds of this workload",
             "error_reference": "FP64 build of the plain kernels on the same inputs, diffusion with the plain "
                                "estimator's mu_e",
             "plain": {"ms": t_plain, "gdofs": dofs / t_plain / 1e6, "err": pe},

@@ -16,9 +16,25 @@ import numpy as np
 from . import capi, workload
 
 GAMMA, RGAS, CE, CMAX = 1.4, 287.0, 0.1, 0.5
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+
+def shipped_weights(workload_name):
+    """Weight file of the network trained on a workload (python -m minisod2d_gb300.learn writes them)."""
+    return os.path.join(DATA, "mlp_%s.bin" % workload_name)
+
+
+def shipped_report(workload_name):
+    import json
+
+    with open(os.path.join(DATA, "%s_report.json" % workload_name)) as f:
+        return json.load(f)
+
+
 # Network trained on the learned_48 workload (48^3 hexes, porder 4, shock-like
-# fields, 64 training seeds; python -m minisod2d_gb300.learn writes it).
-SHIPPED_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "mlp_learned_48.bin")
+# fields, 64 training seeds).  The features and the target depend on the mesh
+# size and the order, so each workload has its own network.
+SHIPPED_WEIGHTS = shipped_weights("learned_48")
 NFEAT = 12
 NPARAMS = 1505
 
@@ -309,10 +325,12 @@ def _main(argv=None):
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--weights", default=None)
-    ap.add_argument("--report", default=None)
+    ap.add_argument("--weights", default=None, help="weight file to write (default data/mlp_<config>.bin)")
+    ap.add_argument("--report", default=None, help="report to write (default data/<config>_report.json)")
     a = ap.parse_args(argv)
     cfg = workload.CONFIGS[a.config]
+    a.weights = a.weights or shipped_weights(a.config)
+    a.report = a.report or os.path.join(DATA, "%s_report.json" % a.config)
     train = list(range(a.ntrain))
     ev = list(range(1000, 1000 + a.neval))
     rep = train_and_evaluate(cfg, train, ev, a.steps, a.batch, a.lr, weights=a.weights)

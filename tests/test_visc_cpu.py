@@ -1,5 +1,6 @@
 """CPU checks of the viscosity estimators' references (no GPU)."""
 import numpy as np
+import pytest
 
 from minisod2d_gb300 import workload
 from oracle import oracle as O
@@ -79,14 +80,15 @@ def test_numpy_features_are_finite():
     assert np.allclose(numax, numax_o, rtol=1e-12)
 
 
-def test_shipped_weight_file_format():
-    """The committed network: magic, sizes and CRC-32 of the weight file."""
+@pytest.mark.parametrize("name", ["learned_48", "combined_96"])
+def test_shipped_weight_file_format(name):
+    """The committed networks: magic, sizes and CRC-32 of the weight files."""
     import struct
     import zlib
 
     from minisod2d_gb300 import learn
 
-    b = open(learn.SHIPPED_WEIGHTS, "rb").read()
+    b = open(learn.shipped_weights(name), "rb").read()
     assert b[:8] == b"MSODMLP1"
     ver, nin, nh, npar = struct.unpack("<4i", b[8:24])
     assert (ver, nin, nh, npar) == (1, 12, 32, mlp_ref.NPARAMS)
