@@ -294,10 +294,12 @@ int msod_mlp_features(int porder, int nelem, int npoin, const int *connec, const
 typedef struct msod_mlp msod_mlp;
 int msod_mlp_create(msod_mlp **out, uint64_t seed);
 int msod_mlp_destroy(msod_mlp *m);
-/* Adam on mean-squared error of y = nu/nu_max over nsamples device pairs
- * (feat[nsamples*12], target[nsamples]); batch samples drawn per step from
- * `seed`; the feature normalisation is set from the training data.
- * loss_host (steps floats) may be NULL.  Synchronous. */
+/* Adam over nsamples device pairs (feat[nsamples*12], target[nsamples] =
+ * y = nu/nu_max of the plain estimator).  The network's output s is a number
+ * of decades (y = 10^-s); the loss is the mean-squared error of s against
+ * -log10(max(target, 1e-12)).  Batch samples are drawn per step from `seed`;
+ * the feature normalisation and training ranges are set from the training
+ * data.  loss_host (steps floats) may be NULL.  Synchronous. */
 int msod_mlp_train(msod_mlp *m, const float *feat, const float *target, int nsamples, int steps,
                    int batch, float lr, uint64_t seed, float *loss_host, void *stream);
 /* Batch gradient of the loss at the current weights (for gradient checks). */
@@ -305,8 +307,8 @@ int msod_mlp_gradient(msod_mlp *m, const float *feat, const float *target, const
                       float *grad_host, void *stream);
 int msod_mlp_get_params(const msod_mlp *m, float *params_host, float *norm_host);
 int msod_mlp_set_params(msod_mlp *m, const float *params_host, const float *norm_host);
-/* y = network output clipped to [0,1], nu = y*numax (if numax given), flag = 1
- * where a feature lies outside the training range. */
+/* y = 10^-s in (0, 1] from the network output s >= 0, nu = y*numax (if numax
+ * given), flag = 1 where a feature lies outside the training range. */
 int msod_mlp_predict(const msod_mlp *m, const float *feat, const float *numax_elem, int nelem, float *y,
                      float *nu_elem, int *flag, void *stream);
 /* Weight file with a CRC-32; a failed check returns MSOD_ERR_BAD_MODEL. */
