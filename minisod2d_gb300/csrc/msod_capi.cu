@@ -140,14 +140,16 @@ static int convec_impl(int porder, int nelem, int npoin, const int *connec, cons
         rc = run_check(porder, nelem, npoin, connec, (const float *)dlx, inv, ai, aj, ak, st);
         if (rc) return rc;
     }
-    TableScratch *tabs = nullptr;  // the convection kernel reads the caller's tables itself
+    TableScratch *tabs = device_tables();
+    if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
     rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
     if (rc) return rc;
     ConvecArgs<real> a;
     a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlx;
     a.invAtoIJK = inv; a.AtoI = ai; a.AtoJ = aj; a.AtoK = ak;
     a.u = u; a.q = q; a.rho = rho; a.pr = pr; a.E = E; a.Rmass = Rmass; a.Rmom = Rmom; a.Rener = Rener;
-    rc = cuda_status(launch_convec_plain<real>(porder, a, tabs, st), "convection kernel launch");
+    rc = cuda_status(launch_table_prep<real>(porder, a, tabs, st), "table preparation launch");
+    if (!rc) rc = cuda_status(launch_convec_plain<real>(porder, a, tabs, st), "convection kernel launch");
     if (!rc && checked_mode()) rc = cuda_status(cudaStreamSynchronize(st), "convection kernel");
     return rc;
 }

@@ -36,8 +36,31 @@
 #include "msod_device.cuh"
 #include "msod_kernels.h"
 
+#ifndef CONVEC_MINB
+#define CONVEC_MINB 4
+#endif
+
 namespace msod {
 namespace {
+
+// 1-D derivative matrices of the current call, per porder (copied from the
+// per-call table area before the launch): with one thread per line, the
+// contraction FMAs take their coefficients as constant-bank operands.
+__constant__ float c_CDf[MSOD_MAX_PORDER + 1][kTableDMax];
+__constant__ double c_CDd[MSOD_MAX_PORDER + 1][kTableDMax];
+
+template <typename real>
+__device__ __forceinline__ real cCD(int P, int i);
+template <>
+__device__ __forceinline__ float cCD<float>(int P, int i)
+{
+    return c_CDf[P][i];
+}
+template <>
+__device__ __forceinline__ double cCD<double>(int P, int i)
+{
+    return c_CDd[P][i];
+}
 
 template <int Q, typename real>
 __device__ __forceinline__ real pick(const real (&a)[Q], int i)
@@ -101,8 +124,9 @@ __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *_
         const int r = r0 + rr;
         const bool ok = (R * S == Q) || r < Q;
         const int rc = ok ? r : 0;
+        if (S > 1)
 #pragma unroll
-        for (int c = 0; c < Q; ++c) Dm[rr][c] = sD[(DIR * Q + rc) * Q + c];
+            for (int c = 0; c < Q; ++c) Dm[rr][c] = sD[(DIR * Q + rc) * Q + c];
         const int a = sPerm[line_lat<DIR, Q>(la, lb, rc)];
         gidx[rr] = a;
         const real *hp = He + ((size_t)(e < nelem ? e : 0) * N + a) * 9 + DIR * 3;
@@ -134,7 +158,7 @@ __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *_
         for (int rr = 0; rr < R; ++rr) {
             real s = (real)0;
 #pragma unroll
-            for (int c = 0; c < Q; ++c) s = fma(Dm[rr][c], v[c], s);
+            for (int c = 0; c < Q; ++c) s = fma(S == 1 ? cCD<real>(P, (DIR * Q + rr) * Q + c) : Dm[rr][c], v[c], s);
             d[rr] = s;
         }
     };
@@ -246,8 +270,17 @@ __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *_
     }
 }
 
+// Blocks per SM the register budget is sized for: four 128-thread blocks (128
+// registers) when the derivative matrices are constant-bank operands.
 template <typename real, int P>
-__global__ void __launch_bounds__(LineGeom<real, P>::NT)
+constexpr int convec_minb()
+{
+    using G = LineGeom<real, P>;
+    return (sizeof(real) == 4 && G::S == 1 && G::NT <= 128 && P >= 3) ? CONVEC_MINB : 1;
+}
+
+template <typename real, int P>
+__global__ void __launch_bounds__(LineGeom<real, P>::NT, convec_minb<real, P>())
     convec_kernel(int nelem, int npoin, const int *__restrict__ connec, const real *__restrict__ He,
                   const real *__restrict__ gpvol, const real *__restrict__ dlxigp_ip,
                   const int *__restrict__ invAtoIJK, const int *__restrict__ AtoI,
@@ -323,13 +356,23 @@ constexpr size_t convec_smem()
 }
 
 template <typename real, int P>
-cudaError_t launch_convec_p(const ConvecArgs<real> &a, cudaStream_t st)
+cudaError_t launch_convec_p(const ConvecArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
     using G = LineGeom<real, P>;
     constexpr size_t smem = convec_smem<real, P>();
     static_assert(smem <= 227 * 1024, "shared memory budget");
     cudaError_t err = cudaFuncSetAttribute(convec_kernel<real, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
+    if (G::S == 1) {
+        if (!tabs) return cudaErrorInvalidValue;
+        if (sizeof(real) == 4)
+            err = cudaMemcpyToSymbolAsync(c_CDf, table_D<float>(tabs), sizeof(float) * 3 * G::Q * G::Q,
+                                          sizeof(float) * kTableDMax * P, cudaMemcpyDeviceToDevice, st);
+        else
+            err = cudaMemcpyToSymbolAsync(c_CDd, table_D<double>(tabs), sizeof(double) * 3 * G::Q * G::Q,
+                                          sizeof(double) * kTableDMax * P, cudaMemcpyDeviceToDevice, st);
+        if (err != cudaSuccess) return err;
+    }
     const unsigned grid = (unsigned)((a.nelem + G::NE - 1) / G::NE);
     convec_kernel<real, P><<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.dlxigp_ip,
                                                       a.invAtoIJK, a.AtoI, a.AtoJ, a.AtoK, a.u, a.q, a.rho,
@@ -340,17 +383,17 @@ cudaError_t launch_convec_p(const ConvecArgs<real> &a, cudaStream_t st)
 }  // namespace
 
 template <typename real>
-cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, const TableScratch *, cudaStream_t st)
+cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
     switch (porder) {
-    case 1: return launch_convec_p<real, 1>(a, st);
-    case 2: return launch_convec_p<real, 2>(a, st);
-    case 3: return launch_convec_p<real, 3>(a, st);
-    case 4: return launch_convec_p<real, 4>(a, st);
-    case 5: return launch_convec_p<real, 5>(a, st);
-    case 6: return launch_convec_p<real, 6>(a, st);
-    case 7: return launch_convec_p<real, 7>(a, st);
-    case 8: return launch_convec_p<real, 8>(a, st);
+    case 1: return launch_convec_p<real, 1>(a, tabs, st);
+    case 2: return launch_convec_p<real, 2>(a, tabs, st);
+    case 3: return launch_convec_p<real, 3>(a, tabs, st);
+    case 4: return launch_convec_p<real, 4>(a, tabs, st);
+    case 5: return launch_convec_p<real, 5>(a, tabs, st);
+    case 6: return launch_convec_p<real, 6>(a, tabs, st);
+    case 7: return launch_convec_p<real, 7>(a, tabs, st);
+    case 8: return launch_convec_p<real, 8>(a, tabs, st);
     default: return cudaErrorInvalidValue;
     }
 }
