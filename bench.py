@@ -493,6 +493,7 @@ def variant_learned(reps):
     r["workload"] = "learned_48: 48^3 hexes, porder 4, shock-like fields, held-out seed 2024"
     r["speedup_estimator_plus_diffusion"] = r["ms_plain_estimator_plus_diffusion"] / \
         r["ms_learned_estimator_plus_diffusion"]
+    r["speedup_fused"] = r["ms_plain_estimator_plus_diffusion"] / r["ms_fused_learned_diffusion"]
     return r
 
 

@@ -31,6 +31,7 @@
 
 #include "msod_device.cuh"
 #include "msod_kernels.h"
+#include "msod_mlp.cuh"
 
 namespace msod {
 namespace {
@@ -147,7 +148,23 @@ constexpr size_t diffu_smem_bytes()
 template <typename real, int P>
 using DiffuGeom = LineGeom<real, P, necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES, (int)sizeof(real), 200 * 1024)>;
 
-template <class G, bool NUE>
+// Viscosity source of the diffusion kernel.
+enum { VISC_MU_E = 0, VISC_NU_ELEM = 1, VISC_NET = 2 };
+
+// Shared memory of the network mode: transposed weights (lane j of a warp
+// reads unit j of each input: conflict-free), the group's features and
+// per-element inputs, and the viscosity per element.
+constexpr int kNetW1T = 0, kNetB1 = kNetW1T + kMlpIn * kMlpH, kNetW2T = kNetB1 + kMlpH,
+              kNetB2 = kNetW2T + kMlpH * kMlpH, kNetW3 = kNetB2 + kMlpH, kNetB3 = kNetW3 + kMlpH,
+              kNetWords = kNetB3 + 1;
+
+template <class G>
+constexpr size_t net_smem_floats()
+{
+    return (size_t)kNetWords + G::NE * (kMlpIn + 4);
+}
+
+template <class G, int VISC>
 __global__ void __launch_bounds__(G::NT)
     diffu_kernel(int nelem, int npoin, int ngroups, const int *__restrict__ connec,
                  const typename G::real *__restrict__ He, const typename G::real *__restrict__ gpvol,
@@ -156,7 +173,7 @@ __global__ void __launch_bounds__(G::NT)
                  const typename G::real *__restrict__ Tem, const typename G::real *__restrict__ mu_fluid,
                  const typename G::real *__restrict__ mu_e, const typename G::real *__restrict__ mu_sgs,
                  const typename G::real *__restrict__ nu_elem, typename G::real *__restrict__ Rmass,
-                 typename G::real *__restrict__ Rmom, typename G::real *__restrict__ Rener)
+                 typename G::real *__restrict__ Rmom, typename G::real *__restrict__ Rener, DiffuNet net)
 {
     using real = typename G::real;
     constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT, NPL = G::NPL;
@@ -167,12 +184,89 @@ __global__ void __launch_bounds__(G::NT)
     int *sNode = reinterpret_cast<int *>(sX + 3 * NX * NPL);  // [2][NPL]
     int *sPerm = sNode + 2 * NPL;
     int *sLat = sPerm + N;
+    float *sNet = reinterpret_cast<float *>(sLat + N);  // network mode: weights, then per-group data
+    float *sFeat = sNet + kNetWords;                      // [NE][12]
+    float *sInfo = sFeat + NE * kMlpIn;                   // [NE][4]: numax, flag, fallback nu, nu
 
     const int tid = threadIdx.x;
     for (int i = tid; i < N; i += NT) {
         sPerm[i] = tabs->perm[i];
         sLat[i] = tabs->lat[i];
     }
+    if (VISC == VISC_NET) {
+        for (int i = tid; i < kMlpParams; i += NT) {
+            const float w = __half2float(net.wh[i]);
+            int d;
+            if (i < kOffB1) d = kNetW1T + (i % kMlpIn) * kMlpH + i / kMlpIn;          // W1[j][k] -> [k][j]
+            else if (i < kOffW2) d = kNetB1 + (i - kOffB1);
+            else if (i < kOffB2) d = kNetW2T + ((i - kOffW2) % kMlpH) * kMlpH + (i - kOffW2) / kMlpH;
+            else if (i < kOffW3) d = kNetB2 + (i - kOffB2);
+            else if (i < kOffB3) d = kNetW3 + (i - kOffW3);
+            else d = kNetB3;
+            sNet[d] = w;
+        }
+    }
+    // Network mode: the group's features and per-element inputs, loaded one
+    // group ahead into registers (thread t < 12 NE: one feature; t < NE also
+    // numax, flag, fallback nu).
+    float pf_feat = 0.0f, pf_numax = 0.0f, pf_flag = 0.0f, pf_fb = 0.0f;
+    auto load_net = [&](int g) {
+        if (VISC != VISC_NET) return;
+        if (tid < NE * kMlpIn) {
+            const int e = g * NE + tid / kMlpIn;
+            pf_feat = e < nelem ? ldg(net.feat + (size_t)e * kMlpIn + tid % kMlpIn) : 0.0f;
+        }
+        if (tid < NE) {
+            const int e = g * NE + tid;
+            const bool ok = e < nelem;
+            pf_numax = ok ? ldg(net.numax + e) : 0.0f;
+            pf_flag = ok ? (float)ldg(net.flag + e) : 0.0f;
+            pf_fb = (ok && pf_flag != 0.0f) ? ldg(net.nu_fb + e) : 0.0f;
+        }
+    };
+    auto store_net = [&]() {
+        if (VISC != VISC_NET) return;
+        if (tid < NE * kMlpIn) sFeat[tid] = pf_feat;
+        if (tid < NE) {
+            sInfo[tid * 4 + 0] = pf_numax;
+            sInfo[tid * 4 + 1] = pf_flag;
+            sInfo[tid * 4 + 2] = pf_fb;
+        }
+    };
+    // One warp per element: the network (same operation order as the
+    // prediction kernel), or the plain estimator's value for flagged elements.
+    auto run_net = [&](int g) {
+        if (VISC != VISC_NET) return;
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int el = warp; el < NE; el += NT / 32) {
+            const int e = g * NE + el;
+            float nu = 0.0f;
+            if (e < nelem) {
+                if (sInfo[el * 4 + 1] != 0.0f) {
+                    nu = sInfo[el * 4 + 2];
+                } else {
+                    float a1 = sNet[kNetB1 + lane];
+#pragma unroll
+                    for (int k = 0; k < kMlpIn; ++k) {
+                        const float xk = (sFeat[el * kMlpIn + k] - ldg(&net.norm->mean[k])) * ldg(&net.norm->inv_std[k]);
+                        a1 = fmaf(sNet[kNetW1T + k * kMlpH + lane], xk, a1);
+                    }
+                    const float h1 = silu(a1);
+                    float a2 = sNet[kNetB2 + lane];
+#pragma unroll
+                    for (int k = 0; k < kMlpH; ++k)
+                        a2 = fmaf(sNet[kNetW2T + k * kMlpH + lane], __shfl_sync(0xffffffffu, h1, k), a2);
+                    const float h2 = silu(a2);
+                    float z = sNet[kNetB3];
+#pragma unroll
+                    for (int j = 0; j < kMlpH; ++j) z = fmaf(sNet[kNetW3 + j], __shfl_sync(0xffffffffu, h2, j), z);
+                    nu = y_from_s(softplus(z)) * sInfo[el * 4 + 0];
+                }
+                if (lane == 0 && net.nu_out) net.nu_out[e] = nu;
+            }
+            if (lane == 0) sInfo[el * 4 + 3] = nu;
+        }
+    };
 
     auto load_ids = [&](int g, int (&ids)[IPT]) {
 #pragma unroll
@@ -212,7 +306,7 @@ __global__ void __launch_bounds__(G::NT)
             const int o = el * ES + sLat[a];
             const bool ok = e < nelem;
             const size_t idx = ok ? (size_t)a * nelem + e : 0;
-            if (!NUE) cp_async_elem(dst + D_MUE * NPL + o, mu_e + idx, ok);
+            if (VISC == VISC_MU_E) cp_async_elem(dst + D_MUE * NPL + o, mu_e + idx, ok);
             cp_async_elem(dst + D_MUS * NPL + o, mu_sgs + idx, ok);
         }
         cp_async_commit();
@@ -240,6 +334,7 @@ __global__ void __launch_bounds__(G::NT)
     store_ids(ids, sNode);
     __syncthreads();
     gather(g, sNode, sF);
+    load_net(g);
     int gn = g + stride;
     if (gn < ngroups) load_ids(gn, ids);
 
@@ -252,12 +347,15 @@ __global__ void __launch_bounds__(G::NT)
         real Hm[IPT][9], gv[IPT];
         load_metric(g, Hm, gv);
         if (gn < ngroups) store_ids(ids, sNode + (s ^ 1) * NPL);
+        store_net();
         cp_async_wait_all();
         __syncthreads();
         if (gn < ngroups) {
             gather(gn, sNode + (s ^ 1) * NPL, sF + (s ^ 1) * NDF * NPL);
             if (gn + stride < ngroups) load_ids(gn + stride, ids);
+            load_net(gn);
         }
+        run_net(g);
         if (lt.active) {
             grad_pass<G, 0>(lt, sFs, sX);
             grad_pass<G, 1>(lt, sFs, sX);
@@ -280,7 +378,9 @@ __global__ void __launch_bounds__(G::NT)
             const real uu[3] = {sFs[D_U0 * NPL + o], sFs[D_U1 * NPL + o], sFs[D_U2 * NPL + o]};
             const int ee = g * NE + el;
             const real muf = sFs[D_MUF * NPL + o], ms = sFs[D_MUS * NPL + o];
-            const real me = NUE ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0) : sFs[D_MUE * NPL + o];
+            const real me = VISC == VISC_NU_ELEM ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0)
+                            : VISC == VISC_NET  ? r * (real)sInfo[el * 4 + 3]
+                                                : sFs[D_MUE * NPL + o];
             // Hm[k][j*3+ii] = He(ii, j)
             real gR[3], gT[3], gU[3][3];
 #pragma unroll
@@ -324,14 +424,14 @@ __global__ void __launch_bounds__(G::NT)
     }
 }
 
-template <typename real, int P, bool NUE>
+template <typename real, int P, int VISC>
 cudaError_t launch_diffu_pn(const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
     using G = DiffuGeom<real, P>;
-    constexpr size_t smem = diffu_smem_bytes<G>();
+    constexpr size_t smem = diffu_smem_bytes<G>() + (VISC == VISC_NET ? net_smem_floats<G>() * sizeof(float) : 0);
     static_assert(smem <= 227 * 1024, "shared memory budget");
     static_assert(G::NE >= 1, "element group");
-    auto kern = diffu_kernel<G, NUE>;
+    auto kern = diffu_kernel<G, VISC>;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     if (sizeof(real) == 4)
@@ -345,15 +445,19 @@ cudaError_t launch_diffu_pn(const DiffuArgs<real> &a, const TableScratch *tabs, 
     const int grid = persistent_grid(kern, G::NT, smem, ngroups);
     if (grid <= 0) return cudaErrorInvalidConfiguration;
     kern<<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, ngroups, a.connec, a.He, a.gpvol, tabs, a.Cp, a.Pr, a.rho, a.u,
-                                    a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.nu_elem, a.Rmass, a.Rmom, a.Rener);
+                                    a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.nu_elem, a.Rmass, a.Rmom, a.Rener, a.net);
     return cudaGetLastError();
 }
 
 template <typename real, int P>
 cudaError_t launch_diffu_p(const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
-    if (a.nu_elem) return launch_diffu_pn<real, P, true>(a, tabs, st);
-    return launch_diffu_pn<real, P, false>(a, tabs, st);
+    if (a.net.feat) {
+        if (sizeof(real) != 4) return cudaErrorInvalidValue;  // the network path is FP32
+        return launch_diffu_pn<real, P, VISC_NET>(a, tabs, st);
+    }
+    if (a.nu_elem) return launch_diffu_pn<real, P, VISC_NU_ELEM>(a, tabs, st);
+    return launch_diffu_pn<real, P, VISC_MU_E>(a, tabs, st);
 }
 
 }  // namespace

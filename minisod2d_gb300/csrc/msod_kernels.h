@@ -52,11 +52,26 @@ struct ConvecArgs : ElementArgs<real> {
     real *Rmass, *Rmom, *Rener;
 };
 
+struct MlpNorm;
+
+// The per-element network evaluated in the diffusion prologue (FP32 kernels):
+// nu(e) = numax(e) 10^-s(feat(e)) where flag(e) == 0, nu_fb(e) (the plain
+// estimator's value) where flag(e) != 0; nu_out, if set, receives nu.
+struct DiffuNet {
+    const float *feat;
+    const __half *wh;
+    const MlpNorm *norm;
+    const float *numax, *nu_fb;
+    const int *flag;
+    float *nu_out;
+};
+
 template <typename real>
 struct DiffuArgs : ElementArgs<real> {
     real Cp, Pr;
     const real *rho, *u, *Tem, *mu_fluid, *mu_e, *mu_sgs;
     const real *nu_elem;  // if set: mu_e(e, a) = rho(a) * nu_elem[e] and mu_e is not read
+    DiffuNet net{};       // if net.feat is set: nu from the network, mu_e and nu_elem are not read
     real *Rmass, *Rmom, *Rener;
 };
 
@@ -141,6 +156,8 @@ struct FeatureArgs {
     float Rgas, gamma, cmax;
     const EntropyStats *stats;
     float *feat, *numax;
+    const MlpNorm *norm;  // with flag: flag[e] = 1 where a feature leaves the training range
+    int *flag;
 };
 
 cudaError_t launch_entropy_stats(int npoin, const float *rho, const float *p_or_T, float Rgas, float gamma,

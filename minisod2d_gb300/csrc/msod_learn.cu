@@ -135,12 +135,29 @@ int msod_entropy_viscosity(int porder, int nelem, int npoin, const int *connec, 
     return cuda_rc(launch_entropy_visc(porder, a, st), "entropy viscosity launch");
 }
 
+// Features (and, with norm, the out-of-range flags of a trained network).
+static int features_impl(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
+                         const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
+                         const int *gmshAtoK, const float *rho, const float *u, const float *p_or_T, float Rgas,
+                         float gamma, float cmax, float *feat, float *numax_elem, const MlpNorm *norm, int *flag,
+                         void *stream);
+
 int msod_mlp_features(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
                       const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
                       const int *gmshAtoK, const float *rho, const float *u, const float *p_or_T, float Rgas,
                       float gamma, float cmax, float *feat, float *numax_elem, void *stream)
 {
     clear_error();
+    return features_impl(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                         rho, u, p_or_T, Rgas, gamma, cmax, feat, numax_elem, nullptr, nullptr, stream);
+}
+
+static int features_impl(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
+                         const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
+                         const int *gmshAtoK, const float *rho, const float *u, const float *p_or_T, float Rgas,
+                         float gamma, float cmax, float *feat, float *numax_elem, const MlpNorm *norm, int *flag,
+                         void *stream)
+{
     int rc = geometry_ok(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK);
     if (rc) return rc;
     if (!rho || !u || !p_or_T || !feat) return set_error(MSOD_ERR_INVALID_ARG, "NULL field or feature array");
@@ -158,7 +175,7 @@ int msod_mlp_features(int porder, int nelem, int npoin, const int *connec, const
     FeatureArgs fa{};
     fa.nelem = nelem; fa.npoin = npoin; fa.connec = connec; fa.He = He; fa.gpvol = gpvol; fa.tabs = tabs;
     fa.rho = rho; fa.u = u; fa.p_or_T = p_or_T; fa.Rgas = Rgas; fa.gamma = gamma; fa.cmax = cmax; fa.stats = stats;
-    fa.feat = feat; fa.numax = numax_elem;
+    fa.feat = feat; fa.numax = numax_elem; fa.norm = norm; fa.flag = flag;
     return cuda_rc(launch_features(porder, fa, st), "feature launch");
 }
 
@@ -398,6 +415,47 @@ int msod_learned_viscosity(const msod_mlp *m, int porder, int nelem, int npoin, 
     a.rho = rho; a.u = u; a.p_or_T = p_or_T; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
     a.normalise = 1; a.stats = stats; a.only = fl; a.mu_e = nullptr; a.nu = nu_elem; a.numax = nullptr;
     return cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
+}
+
+int msod_diffusion_ijk_learned(const msod_mlp *m, int porder, int nelem, int npoin, const int *connec,
+                               const float *He, const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK,
+                               const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK, float Cp, float Pr,
+                               const float *rho, const float *u, const float *Tem, const float *mu_fluid,
+                               const float *mu_sgs, float Rgas, float gamma, float ce, float cmax, float *Rmass,
+                               float *Rmom, float *Rener, float *nu_elem, int *flag, void *stream)
+{
+    clear_error();
+    if (!m) return set_error(MSOD_ERR_INVALID_ARG, "NULL network");
+    if (!m->has_norm) return set_error(MSOD_ERR_BAD_MODEL, "the network has no training ranges (train or load it)");
+    if (!(Rgas > 0.0f)) return set_error(MSOD_ERR_INVALID_ARG, "Rgas must be positive (p = rho Rgas Tem)");
+    int rc = geometry_ok(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK);
+    if (rc) return rc;
+    if (!rho || !u || !Tem) return set_error(MSOD_ERR_INVALID_ARG, "NULL field");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float *feat = static_cast<float *>(scratch(SLOT_FEAT, sizeof(float) * kMlpIn * (size_t)nelem));
+    float *numax = static_cast<float *>(scratch(SLOT_NUMAX, sizeof(float) * (size_t)nelem));
+    float *nu_fb = static_cast<float *>(scratch(SLOT_NU, sizeof(float) * (size_t)nelem));
+    int *fl = flag ? flag : static_cast<int *>(scratch(SLOT_FLAG, sizeof(int) * (size_t)nelem));
+    if (!feat || !numax || !nu_fb || !fl) return set_error(MSOD_ERR_CUDA, "could not allocate per-element scratch");
+    // 1. features and the out-of-range flags
+    rc = features_impl(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                       rho, u, Tem, Rgas, gamma, cmax, feat, numax, m->norm, fl, stream);
+    if (rc) return rc;
+    // 2. the plain estimator on the flagged elements only (per-element fallback)
+    EntropyStats *stats = static_cast<EntropyStats *>(scratch(SLOT_STATS, sizeof(EntropyStats)));
+    ViscArgs a{};
+    a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlxigp_ip;
+    a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
+    a.rho = rho; a.u = u; a.p_or_T = Tem; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
+    a.normalise = 1; a.stats = stats; a.only = fl; a.mu_e = nullptr; a.nu = nu_fb; a.numax = nullptr;
+    rc = cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
+    if (rc) return rc;
+    // 3. the diffusion, with the network evaluated in its prologue
+    DiffuNet net{};
+    net.feat = feat; net.wh = m->wh; net.norm = m->norm; net.numax = numax; net.nu_fb = nu_fb; net.flag = fl;
+    net.nu_out = nu_elem;
+    return diffusion_with_net(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
+                              gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_sgs, net, Rmass, Rmom, Rener, stream);
 }
 
 }  // extern "C"

@@ -37,18 +37,9 @@
 
 #include "msod_device.cuh"
 #include "msod_kernels.h"
+#include "msod_mlp.cuh"
 
 namespace msod {
-
-__device__ __forceinline__ float silu(float a) { return a / (1.0f + __expf(-a)); }
-__device__ __forceinline__ float sigmoidf_(float a) { return 1.0f / (1.0f + __expf(-a)); }
-__device__ __forceinline__ float softplus(float z) { return z > 20.0f ? z : log1pf(__expf(z)); }
-// Heavy-tailed non-negative features enter as logarithms (offset 1e-12).
-__device__ __forceinline__ float flog(float v) { return logf(fmaxf(v, 0.0f) + 1e-12f); }
-// The network's output s >= 0 is a number of decades: y = 10^-s.  Targets y
-// are mapped to s = -log10(max(y, 1e-12)) for the loss.
-__device__ __forceinline__ float y_from_s(float s) { return exp10f(-s); }
-__device__ __forceinline__ float s_from_y(float y) { return -log10f(fminf(fmaxf(y, 1e-12f), 1.0f)); }
 
 namespace {
 
@@ -67,7 +58,8 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
                     const float *__restrict__ gpvol, const TableScratch *__restrict__ tabs,
                     const float *__restrict__ rho, const float *__restrict__ u, const float *__restrict__ p_or_T,
                     float Rgas, float gamma, float cmax, const EntropyStats *__restrict__ st,
-                    float *__restrict__ feat, float *__restrict__ numax_out)
+                    float *__restrict__ feat, float *__restrict__ numax_out, const MlpNorm *__restrict__ norm,
+                    int *__restrict__ flag)
 {
     constexpr int Q = P + 1, N = Q * Q * Q, kFeatWarps = feat_warps<P>();
     __shared__ float sv[kFeatWarps][5][N];  // rho, p, u0, u1, u2 by gmsh node
@@ -179,6 +171,12 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
     f[10] = flog((emax - emin) / neta);
     f[11] = flog(defect / (neta * (umean + cmean)));
     if (numax_out) numax_out[e] = cmax * h * spdmax;
+    if (flag) {  // outside the network's training range: the plain estimator takes over
+        int out = 0;
+        for (int k = 0; k < kMlpIn; ++k)
+            if (!(f[k] >= norm->fmin[k] && f[k] <= norm->fmax[k])) out = 1;
+        flag[e] = out;
+    }
 }
 
 template <int P>
@@ -188,7 +186,7 @@ cudaError_t features_p(const FeatureArgs &a, cudaStream_t st)
     const unsigned grid = (unsigned)((a.nelem + kFeatWarps - 1) / kFeatWarps);
     features_kernel<P><<<grid, 32 * kFeatWarps, 0, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.tabs, a.rho,
                                                          a.u, a.p_or_T, a.Rgas, a.gamma, a.cmax, a.stats, a.feat,
-                                                         a.numax);
+                                                         a.numax, a.norm, a.flag);
     return cudaGetLastError();
 }
 

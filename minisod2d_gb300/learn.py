@@ -148,6 +148,22 @@ def learned_viscosity(mlp, dev, nu=None, flag=None, ce=CE, cmax=CMAX, gamma=GAMM
     return nu, flag
 
 
+def diffusion_learned(mlp, dev, out=None, nu=None, flag=None, ce=CE, cmax=CMAX, gamma=GAMMA, rgas=RGAS,
+                      stream=None):
+    """Diffusion with the network evaluated in the diffusion kernel's prologue
+    (features from rho, u and p = rho Rgas T; plain-estimator fallback per
+    element).  Returns the residuals, the viscosity used and the fallback flags."""
+    import torch
+
+    out = out or (dev.Dmass, dev.Dmom, dev.Dener)
+    nu = nu if nu is not None else torch.empty(dev.nelem, device=dev.rho.device)
+    flag = flag if flag is not None else torch.empty(dev.nelem, dtype=torch.int32, device=dev.rho.device)
+    capi.call("msod_diffusion_ijk_learned", mlp.h, *_geo(dev), float(dev.cfg.Cp), float(dev.cfg.Pr), _p(dev.rho),
+              _p(dev.u), _p(dev.Tem), _p(dev.mu_fluid), _p(dev.mu_sgs), float(rgas), float(gamma), float(ce),
+              float(cmax), *[_p(o) for o in out], _p(nu), _p(flag), _stream(stream))
+    return out, nu, flag
+
+
 def diffusion_ijk_nu(dev, nu, out=None, stream=None):
     """Diffusion residual with mu_e(e, a) = rho(a) nu(e)."""
     out = out or (dev.Dmass, dev.Dmom, dev.Dener)
@@ -258,6 +274,8 @@ def evaluate(mlp, dev, ybar=None, reps=5):
     r["ms_learned_estimator"] = _event_ms(lambda: learned_viscosity(mlp, dev, nu_lb, flag_b), reps)
     r["ms_plain_estimator_plus_diffusion"] = _event_ms(plain, reps)
     r["ms_learned_estimator_plus_diffusion"] = _event_ms(learned, reps)
+    # the network evaluated in the diffusion prologue (features + fallback + fused diffusion)
+    r["ms_fused_learned_diffusion"] = _event_ms(lambda: diffusion_learned(mlp, dev, out_l, nu_lb, flag_b), reps)
     return r
 
 

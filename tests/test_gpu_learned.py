@@ -202,3 +202,82 @@ def test_shipped_network_on_held_out_learned_48_seed(cuda):
     assert r["nu_rel_l2"] < 0.5 * r["constant_ratio"]["nu_rel_l2"]
     assert r["Rmom_rel_l2"] < 0.01 and r["Rener_rel_l2"] < 0.02
     assert r["fallback_fraction"] < 0.01
+
+
+def _learned_from_T(m, dev):
+    """The separate-kernel path on the same inputs as the fused one (p = rho Rgas T)."""
+    import torch
+
+    nu = torch.empty(dev.nelem, device=dev.rho.device)
+    flag = torch.empty(dev.nelem, dtype=torch.int32, device=dev.rho.device)
+    capi.call("msod_learned_viscosity", m.h, *learn._geo(dev), learn._p(dev.rho), learn._p(dev.u),
+              learn._p(dev.Tem), float(learn.RGAS), float(learn.GAMMA), float(learn.CE), float(learn.CMAX),
+              learn._p(nu), learn._p(flag), torch.cuda.current_stream().cuda_stream)
+    return nu, flag
+
+
+def test_fused_network_in_diffusion_prologue_equals_separate_kernels(cuda):
+    """The network evaluated in the diffusion prologue gives the viscosity of the
+    separate prediction kernel and the same residuals.  (Not bit for bit: the
+    entropy normalisation n_eta comes from an FP64 atomic sum over the nodes,
+    so two runs of either path differ in the last bits.)"""
+    import torch
+
+    host, dev = _dev(cuda, 4, 6, seed=2)
+    m = learn.Mlp()
+    m.load(learn.shipped_weights("learned_48"))
+    nu_ref, flag_ref = _learned_from_T(m, dev)
+    ref = [torch.empty_like(x) for x in (dev.Dmass, dev.Dmom, dev.Dener)]
+    learn.diffusion_ijk_nu(dev, nu_ref, ref)
+    out = [torch.empty_like(x) for x in ref]
+    _, nu, flag = learn.diffusion_learned(m, dev, out)
+    print("FUSED fallback %d of %d" % (int(flag.sum()), dev.nelem))
+    assert torch.equal(flag, flag_ref)
+    a, b = nu.cpu().numpy(), nu_ref.cpu().numpy()
+    assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30)) < 1e-5
+    for a, b in zip(out, ref):
+        assert refimpl.rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
+
+
+def test_fused_network_fallback(cuda):
+    """Every element outside the training range: the fused path uses the plain estimator."""
+    import torch
+
+    host, dev = _dev(cuda, 4, 3, seed=4)
+    m = learn.Mlp(seed=1)
+    w, norm = m.params()
+    norm = norm.copy()
+    norm[24:36] = 1e30
+    norm[36:48] = -1e30
+    m.set_params(None, norm)
+    out = [torch.empty_like(x) for x in (dev.Dmass, dev.Dmom, dev.Dener)]
+    _, nu, flag = learn.diffusion_learned(m, dev, out)
+    assert int(flag.sum()) == dev.nelem
+    # plain estimator on the same inputs (p = rho Rgas T)
+    mu = torch.empty(dev.nelem * dev.cfg.nnode, device=cuda)
+    nu_p = torch.empty(dev.nelem, device=cuda)
+    nm = torch.empty(dev.nelem, device=cuda)
+    capi.call("msod_entropy_viscosity", *learn._geo(dev), learn._p(dev.rho), learn._p(dev.u), learn._p(dev.pr),
+              float(learn.GAMMA), float(learn.CE), float(learn.CMAX), 1, learn._p(mu), learn._p(nu_p), learn._p(nm),
+              torch.cuda.current_stream().cuda_stream)
+    assert refimpl.rel_l2(nu.cpu().numpy(), nu_p.cpu().numpy()) < 1e-5
+
+
+def test_fused_network_without_fallback(cuda):
+    """No element falls back (unbounded training ranges): every viscosity comes
+    from the network evaluated in the prologue and matches the prediction kernel."""
+    import torch
+
+    host, dev = _dev(cuda, 4, 5, seed=6)
+    m = learn.Mlp(seed=3)
+    w, norm = m.params()
+    norm = norm.copy()
+    norm[24:36] = -1e30
+    norm[36:48] = 1e30
+    m.set_params(None, norm)
+    nu_ref, flag_ref = _learned_from_T(m, dev)
+    _, nu, flag = learn.diffusion_learned(m, dev)
+    assert int(flag.sum()) == 0 and int(flag_ref.sum()) == 0
+    a, b = nu.cpu().numpy(), nu_ref.cpu().numpy()
+    assert np.all(a > 0)
+    assert np.max(np.abs(a - b) / np.abs(b)) < 1e-5
