@@ -324,18 +324,19 @@ int msod_learned_viscosity(const msod_mlp *m, int porder, int nelem, int npoin, 
                            void *stream);
 /* No counterpart in the reference: full_diffusion_ijk with the artificial
  * viscosity from the network, evaluated per element in the diffusion
- * kernel's prologue (p = rho Rgas Tem for the features, Rgas > 0).  Elements
- * whose features leave the network's training range take the plain
- * estimator's value (computed for those elements only).  nu_elem and flag
- * (nelem each, optional) receive the viscosity used and the fallback flags. */
+ * kernel's prologue.  The features take the pressure p_or_T (Rgas = 0) or
+ * p = rho Rgas T from the temperature p_or_T (Rgas > 0).  Elements whose
+ * features leave the network's training range take the plain estimator's
+ * value (computed for those elements only).  nu_elem and flag (nelem each,
+ * optional) receive the viscosity used and the fallback flags. */
 int msod_diffusion_ijk_learned(const msod_mlp *m, int porder, int nelem, int npoin, const int *connec,
                                const float *He, const float *gpvol, const float *dlxigp_ip,
                                const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
                                const int *gmshAtoK, float Cp, float Pr, const float *rho,
                                const float *u, const float *Tem, const float *mu_fluid,
-                               const float *mu_sgs, float Rgas, float gamma, float ce, float cmax,
-                               float *Rmass, float *Rmom, float *Rener, float *nu_elem, int *flag,
-                               void *stream);
+                               const float *mu_sgs, const float *p_or_T, float Rgas, float gamma,
+                               float ce, float cmax, float *Rmass, float *Rmom, float *Rener,
+                               float *nu_elem, int *flag, void *stream);
 /* full_diffusion_ijk with mu_e(e,a) = rho(a) nu_elem(e): one viscosity value
  * per element instead of the mu_e(nelem,ngaus) array. */
 int msod_diffusion_ijk_nu(int porder, int nelem, int npoin, const int *connec, const float *He,

@@ -72,7 +72,7 @@ SIGNATURES = {
     "msod_mlp_load": [_p, C.c_char_p],
     "msod_learned_viscosity": [_p, _i, _i, _i] + [_p] * 8 + [_p, _p, _p, _f, _f, _f, _f, _p, _p, _p],
     "msod_diffusion_ijk_nu": [_i, _i, _i] + [_p] * 8 + [_f, _f] + [_p] * 9 + [_p],
-    "msod_diffusion_ijk_learned": [_p, _i, _i, _i] + [_p] * 8 + [_f, _f] + [_p] * 5 + [_f] * 4 + [_p] * 6,
+    "msod_diffusion_ijk_learned": [_p, _i, _i, _i] + [_p] * 8 + [_f, _f] + [_p] * 6 + [_f] * 4 + [_p] * 6,
 }
 
 

@@ -226,42 +226,64 @@ __global__ void __launch_bounds__(G::NT)
     };
     auto store_net = [&]() {
         if (VISC != VISC_NET) return;
-        if (tid < NE * kMlpIn) sFeat[tid] = pf_feat;
+        if (tid < NE * kMlpIn) {  // normalised here, as the prediction kernel does
+            const int k = tid % kMlpIn;
+            sFeat[tid] = (pf_feat - ldg(&net.norm->mean[k])) * ldg(&net.norm->inv_std[k]);
+        }
         if (tid < NE) {
             sInfo[tid * 4 + 0] = pf_numax;
             sInfo[tid * 4 + 1] = pf_flag;
             sInfo[tid * 4 + 2] = pf_fb;
         }
     };
-    // One warp per element: the network (same operation order as the
-    // prediction kernel), or the plain estimator's value for flagged elements.
+    // One warp per element (a warp interleaves its elements): the network in
+    // the operation order of the prediction kernel, or the plain estimator's
+    // value for flagged elements.
     auto run_net = [&](int g) {
         if (VISC != VISC_NET) return;
+        constexpr int NW = NT / 32, ELW = (NE + NW - 1) / NW;
         const int lane = tid & 31, warp = tid >> 5;
-        for (int el = warp; el < NE; el += NT / 32) {
-            const int e = g * NE + el;
+        float a1[ELW], h1[ELW], a2[ELW], z[ELW];
+#pragma unroll
+        for (int q = 0; q < ELW; ++q) a1[q] = sNet[kNetB1 + lane];
+#pragma unroll
+        for (int k = 0; k < kMlpIn; ++k) {
+            const float w = sNet[kNetW1T + k * kMlpH + lane];
+#pragma unroll
+            for (int q = 0; q < ELW; ++q) {
+                const int el = min(warp + q * NW, NE - 1);
+                a1[q] = fmaf(w, sFeat[el * kMlpIn + k], a1[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < ELW; ++q) {
+            h1[q] = silu(a1[q]);
+            a2[q] = sNet[kNetB2 + lane];
+        }
+#pragma unroll
+        for (int k = 0; k < kMlpH; ++k) {
+            const float w = sNet[kNetW2T + k * kMlpH + lane];
+#pragma unroll
+            for (int q = 0; q < ELW; ++q) a2[q] = fmaf(w, __shfl_sync(0xffffffffu, h1[q], k), a2[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < ELW; ++q) {
+            h1[q] = silu(a2[q]);  // the second hidden layer's outputs
+            z[q] = sNet[kNetB3];
+        }
+#pragma unroll
+        for (int j = 0; j < kMlpH; ++j) {
+            const float w = sNet[kNetW3 + j];
+#pragma unroll
+            for (int q = 0; q < ELW; ++q) z[q] = fmaf(w, __shfl_sync(0xffffffffu, h1[q], j), z[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < ELW; ++q) {
+            const int el = warp + q * NW, e = g * NE + el;
+            if (el >= NE) continue;
             float nu = 0.0f;
             if (e < nelem) {
-                if (sInfo[el * 4 + 1] != 0.0f) {
-                    nu = sInfo[el * 4 + 2];
-                } else {
-                    float a1 = sNet[kNetB1 + lane];
-#pragma unroll
-                    for (int k = 0; k < kMlpIn; ++k) {
-                        const float xk = (sFeat[el * kMlpIn + k] - ldg(&net.norm->mean[k])) * ldg(&net.norm->inv_std[k]);
-                        a1 = fmaf(sNet[kNetW1T + k * kMlpH + lane], xk, a1);
-                    }
-                    const float h1 = silu(a1);
-                    float a2 = sNet[kNetB2 + lane];
-#pragma unroll
-                    for (int k = 0; k < kMlpH; ++k)
-                        a2 = fmaf(sNet[kNetW2T + k * kMlpH + lane], __shfl_sync(0xffffffffu, h1, k), a2);
-                    const float h2 = silu(a2);
-                    float z = sNet[kNetB3];
-#pragma unroll
-                    for (int j = 0; j < kMlpH; ++j) z = fmaf(sNet[kNetW3 + j], __shfl_sync(0xffffffffu, h2, j), z);
-                    nu = y_from_s(softplus(z)) * sInfo[el * 4 + 0];
-                }
+                nu = sInfo[el * 4 + 1] != 0.0f ? sInfo[el * 4 + 2] : y_from_s(softplus(z[q])) * sInfo[el * 4 + 0];
                 if (lane == 0 && net.nu_out) net.nu_out[e] = nu;
             }
             if (lane == 0) sInfo[el * 4 + 3] = nu;

@@ -421,16 +421,16 @@ int msod_diffusion_ijk_learned(const msod_mlp *m, int porder, int nelem, int npo
                                const float *He, const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK,
                                const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK, float Cp, float Pr,
                                const float *rho, const float *u, const float *Tem, const float *mu_fluid,
-                               const float *mu_sgs, float Rgas, float gamma, float ce, float cmax, float *Rmass,
-                               float *Rmom, float *Rener, float *nu_elem, int *flag, void *stream)
+                               const float *mu_sgs, const float *p_or_T, float Rgas, float gamma, float ce,
+                               float cmax, float *Rmass, float *Rmom, float *Rener, float *nu_elem, int *flag,
+                               void *stream)
 {
     clear_error();
     if (!m) return set_error(MSOD_ERR_INVALID_ARG, "NULL network");
     if (!m->has_norm) return set_error(MSOD_ERR_BAD_MODEL, "the network has no training ranges (train or load it)");
-    if (!(Rgas > 0.0f)) return set_error(MSOD_ERR_INVALID_ARG, "Rgas must be positive (p = rho Rgas Tem)");
     int rc = geometry_ok(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK);
     if (rc) return rc;
-    if (!rho || !u || !Tem) return set_error(MSOD_ERR_INVALID_ARG, "NULL field");
+    if (!rho || !u || !Tem || !p_or_T) return set_error(MSOD_ERR_INVALID_ARG, "NULL field");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     float *feat = static_cast<float *>(scratch(SLOT_FEAT, sizeof(float) * kMlpIn * (size_t)nelem));
     float *numax = static_cast<float *>(scratch(SLOT_NUMAX, sizeof(float) * (size_t)nelem));
@@ -439,14 +439,14 @@ int msod_diffusion_ijk_learned(const msod_mlp *m, int porder, int nelem, int npo
     if (!feat || !numax || !nu_fb || !fl) return set_error(MSOD_ERR_CUDA, "could not allocate per-element scratch");
     // 1. features and the out-of-range flags
     rc = features_impl(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
-                       rho, u, Tem, Rgas, gamma, cmax, feat, numax, m->norm, fl, stream);
+                       rho, u, p_or_T, Rgas, gamma, cmax, feat, numax, m->norm, fl, stream);
     if (rc) return rc;
     // 2. the plain estimator on the flagged elements only (per-element fallback)
     EntropyStats *stats = static_cast<EntropyStats *>(scratch(SLOT_STATS, sizeof(EntropyStats)));
     ViscArgs a{};
     a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlxigp_ip;
     a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
-    a.rho = rho; a.u = u; a.p_or_T = Tem; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
+    a.rho = rho; a.u = u; a.p_or_T = p_or_T; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
     a.normalise = 1; a.stats = stats; a.only = fl; a.mu_e = nullptr; a.nu = nu_fb; a.numax = nullptr;
     rc = cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
     if (rc) return rc;

@@ -148,19 +148,21 @@ def learned_viscosity(mlp, dev, nu=None, flag=None, ce=CE, cmax=CMAX, gamma=GAMM
     return nu, flag
 
 
-def diffusion_learned(mlp, dev, out=None, nu=None, flag=None, ce=CE, cmax=CMAX, gamma=GAMMA, rgas=RGAS,
+def diffusion_learned(mlp, dev, out=None, nu=None, flag=None, ce=CE, cmax=CMAX, gamma=GAMMA, from_T=False,
                       stream=None):
     """Diffusion with the network evaluated in the diffusion kernel's prologue
-    (features from rho, u and p = rho Rgas T; plain-estimator fallback per
-    element).  Returns the residuals, the viscosity used and the fallback flags."""
+    (features from rho, u and the pressure, or p = rho Rgas T with ``from_T``;
+    plain-estimator fallback per element).  Returns the residuals, the
+    viscosity used and the fallback flags."""
     import torch
 
     out = out or (dev.Dmass, dev.Dmom, dev.Dener)
     nu = nu if nu is not None else torch.empty(dev.nelem, device=dev.rho.device)
     flag = flag if flag is not None else torch.empty(dev.nelem, dtype=torch.int32, device=dev.rho.device)
     capi.call("msod_diffusion_ijk_learned", mlp.h, *_geo(dev), float(dev.cfg.Cp), float(dev.cfg.Pr), _p(dev.rho),
-              _p(dev.u), _p(dev.Tem), _p(dev.mu_fluid), _p(dev.mu_sgs), float(rgas), float(gamma), float(ce),
-              float(cmax), *[_p(o) for o in out], _p(nu), _p(flag), _stream(stream))
+              _p(dev.u), _p(dev.Tem), _p(dev.mu_fluid), _p(dev.mu_sgs), _p(dev.Tem if from_T else dev.pr),
+              float(RGAS if from_T else 0.0), float(gamma), float(ce), float(cmax), *[_p(o) for o in out], _p(nu),
+              _p(flag), _stream(stream))
     return out, nu, flag
 
 

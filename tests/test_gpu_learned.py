@@ -230,7 +230,7 @@ def test_fused_network_in_diffusion_prologue_equals_separate_kernels(cuda):
     ref = [torch.empty_like(x) for x in (dev.Dmass, dev.Dmom, dev.Dener)]
     learn.diffusion_ijk_nu(dev, nu_ref, ref)
     out = [torch.empty_like(x) for x in ref]
-    _, nu, flag = learn.diffusion_learned(m, dev, out)
+    _, nu, flag = learn.diffusion_learned(m, dev, out, from_T=True)
     print("FUSED fallback %d of %d" % (int(flag.sum()), dev.nelem))
     assert torch.equal(flag, flag_ref)
     a, b = nu.cpu().numpy(), nu_ref.cpu().numpy()
@@ -251,7 +251,7 @@ def test_fused_network_fallback(cuda):
     norm[36:48] = -1e30
     m.set_params(None, norm)
     out = [torch.empty_like(x) for x in (dev.Dmass, dev.Dmom, dev.Dener)]
-    _, nu, flag = learn.diffusion_learned(m, dev, out)
+    _, nu, flag = learn.diffusion_learned(m, dev, out, from_T=True)
     assert int(flag.sum()) == dev.nelem
     # plain estimator on the same inputs (p = rho Rgas T)
     mu = torch.empty(dev.nelem * dev.cfg.nnode, device=cuda)
@@ -276,8 +276,27 @@ def test_fused_network_without_fallback(cuda):
     norm[36:48] = 1e30
     m.set_params(None, norm)
     nu_ref, flag_ref = _learned_from_T(m, dev)
-    _, nu, flag = learn.diffusion_learned(m, dev)
+    _, nu, flag = learn.diffusion_learned(m, dev, from_T=True)
     assert int(flag.sum()) == 0 and int(flag_ref.sum()) == 0
     a, b = nu.cpu().numpy(), nu_ref.cpu().numpy()
     assert np.all(a > 0)
     assert np.max(np.abs(a - b) / np.abs(b)) < 1e-5
+
+
+def test_fused_network_with_pressure_matches_separate_path(cuda):
+    """With the pressure itself (as the separate path takes it) the shipped
+    network needs no fallback on its own workload's fields.  (Pressure rebuilt
+    as rho Rgas T carries rounding noise where the training fields have an
+    exactly uniform pressure, and every such element falls back.)"""
+    import torch
+
+    cfg = workload.CONFIGS["learned_48"]
+    host = workload.HostCase(workload.Config(cfg.name, cfg.porder, 16, cfg.jitter, cfg.kind, cfg.nmodes, 77))
+    dev = workload.DeviceCase(host, device=cuda)
+    m = learn.Mlp()
+    m.load(learn.shipped_weights("learned_48"))
+    nu_ref, flag_ref = learn.learned_viscosity(m, dev)
+    _, nu, flag = learn.diffusion_learned(m, dev)
+    assert torch.equal(flag, flag_ref)
+    a, b = nu.cpu().numpy(), nu_ref.cpu().numpy()
+    assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30)) < 1e-5
