@@ -8,7 +8,8 @@ Builds a structured mesh (``--nx``^3 hexes, ``--jitter``) with seeded fields
 ``--warmup`` + ``--iters`` times in order.  Kernels: convec, diffu,
 convec_mixed, diffu_mixed (``--precision`` fp16 / bf16), estimator (plain
 entropy viscosity), learned (features + network + fallback, with a freshly
-initialised network unless ``--weights`` names a weight file).
+initialised network unless ``--weights`` names a weight file), diffu_learned
+(the diffusion with the network in its prologue; needs ``--weights``).
 """
 import argparse
 
@@ -46,17 +47,21 @@ def main(argv=None):
             calls.append(lambda: dev.diffu())
         elif k in ("convec_mixed", "diffu_mixed"):
             if out64 is None:
-                out64 = dev.convec_mixed(a.precision)
+                out64 = tuple(torch.empty(n * dev.npoin, dtype=torch.float64, device=dev.He.device)
+                              for n in (1, 3, 1))
             fn = dev.convec_mixed if k == "convec_mixed" else dev.diffu_mixed
             calls.append(lambda fn=fn: fn(a.precision, out=out64))
         elif k == "estimator":
             calls.append(lambda: learn.entropy_viscosity(dev))
-        elif k == "learned":
+        elif k in ("learned", "diffu_learned"):
             if mlp is None:
                 mlp = learn.Mlp()
                 if a.weights:
                     mlp.load(a.weights)
-            calls.append(lambda: learn.learned_viscosity(mlp, dev))
+            if k == "learned":
+                calls.append(lambda: learn.learned_viscosity(mlp, dev))
+            else:
+                calls.append(lambda: learn.diffusion_learned(mlp, dev))
         else:
             raise SystemExit("unknown kernel %r" % k)
     for fn in calls:
