@@ -271,7 +271,8 @@ int msod_fields_recipe(int kind, int nmodes, uint64_t seed, int64_t npoin, const
  * eta = rho/(gamma-1) log(p/rho^gamma), R = div(eta u) - eta div u - u.grad eta,
  * per element nu = min(cmax h max(|u|+c), ce h^2 max|R| / ||eta - mean eta||_inf)
  * with h = (sum gpvol)^(1/3)/porder; mu_e(e,a) = rho(a) nu(e) in the reference's
- * mu_e(nelem,ngaus) layout.  nu_elem / numax_elem (nelem each) may be NULL.
+ * mu_e(nelem,ngaus) layout.  nu_elem / numax_elem (nelem each) may be NULL,
+ * and mu_e may be NULL when nu_elem is given.
  * porder 1..7. */
 int msod_entropy_viscosity(int porder, int nelem, int npoin, const int *connec, const float *He,
                            const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK,
@@ -345,6 +346,30 @@ int msod_diffusion_ijk_nu(int porder, int nelem, int npoin, const int *connec, c
                           float Pr, const float *rho, const float *u, const float *Tem,
                           const float *mu_fluid, const float *nu_elem, const float *mu_sgs,
                           float *Rmass, float *Rmom, float *Rener, void *stream);
+
+/* No counterpart in the reference, whose form is fixed at compile time: the
+ * form that every later msod_convec_ijk / msod_convec_ijk_split /
+ * msod_diffusion_ijk call of the process computes, so that a driver keeps its
+ * two calls and switches precision and artificial viscosity at run time.
+ *   precision  MSOD_PREC_FP32: the plain kernels (default); MSOD_PREC_FP16 /
+ *              MSOD_PREC_BF16: the tensor-core kernels (porder <= 7) write
+ *              FP64 residuals into library buffers, converted into the
+ *              caller's FP32 arrays.
+ *   mu_e_mode  MSOD_MU_E_GIVEN: the caller's mu_e (default); MSOD_MU_E_PLAIN:
+ *              the entropy-viscosity estimator; MSOD_MU_E_LEARNED: the
+ *              network `mlp` (in the FP32 diffusion's prologue) with the
+ *              estimator as per-element fallback.  Both ignore the mu_e
+ *              argument and use p = rho Rgas Tem, gamma = 1.4, Rgas = 287
+ *              (main.f90:52), ce = 0.1, cmax = 0.5 (mod_numerical_params.f90:23-24).
+ * The network is kept by reference and must outlive its use.  The library
+ * buffers are per device and grow with cudaMalloc; calls that overlap on the
+ * GPU race on them. */
+#define MSOD_PREC_FP32 2
+#define MSOD_MU_E_GIVEN 0
+#define MSOD_MU_E_PLAIN 1
+#define MSOD_MU_E_LEARNED 2
+int msod_set_mode(int precision, int mu_e_mode, const msod_mlp *mlp);
+int msod_get_mode(int *precision, int *mu_e_mode);
 
 #ifdef __cplusplus
 }

@@ -25,6 +25,10 @@ MSOD_FIELDS_SMOOTH = 0
 MSOD_FIELDS_SHOCK = 1
 MSOD_PREC_FP16 = 0
 MSOD_PREC_BF16 = 1
+MSOD_PREC_FP32 = 2
+MSOD_MU_E_GIVEN = 0
+MSOD_MU_E_PLAIN = 1
+MSOD_MU_E_LEARNED = 2
 
 _i, _u64, _i64, _f, _d, _p, _sz = C.c_int, C.c_uint64, C.c_int64, C.c_float, C.c_double, C.c_void_p, C.c_size_t
 
@@ -72,6 +76,8 @@ SIGNATURES = {
     "msod_mlp_load": [_p, C.c_char_p],
     "msod_learned_viscosity": [_p, _i, _i, _i] + [_p] * 8 + [_p, _p, _p, _f, _f, _f, _f, _p, _p, _p],
     "msod_diffusion_ijk_nu": [_i, _i, _i] + [_p] * 8 + [_f, _f] + [_p] * 9 + [_p],
+    "msod_set_mode": [_i, _i, _p],
+    "msod_get_mode": [_p, _p],
     "msod_diffusion_ijk_learned": [_p, _i, _i, _i] + [_p] * 8 + [_f, _f] + [_p] * 6 + [_f] * 4 + [_p] * 6,
 }
 

@@ -229,6 +229,7 @@ int msod_finalize(void)
             g_tables[d] = nullptr;
         }
     cudaSetDevice(cur);
+    mode_release();
     return MSOD_OK;
 }
 
@@ -271,6 +272,9 @@ int msod_convec_ijk(int porder, int nelem, int npoin, const int *connec, const f
                     float *Rmom, float *Rener, void *stream)
 {
     (void)Ngp; (void)dNgp; (void)xgp;
+    if (!mode_is_default_convec())
+        return mode_convec(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
+                           gmshAtoK, u, q, rho, pr, E, Rmass, Rmom, Rener, stream);
     return convec_impl<float>(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
                               gmshAtoK, u, q, rho, pr, E, Rmass, Rmom, Rener, stream);
 }
@@ -282,6 +286,9 @@ int msod_convec_ijk_split(int porder, int nelem, int npoin, const int *connec, c
                           const float *E, float *Rmass, float *Rmom, float *Rener, void *stream)
 {
     (void)Ngp; (void)dNgp; (void)xgp;
+    if (!mode_is_default_convec())
+        return mode_convec(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
+                           gmshAtoK, u, q, rho, pr, E, Rmass, Rmom, Rener, stream);
     return convec_impl<float>(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
                               gmshAtoK, u, q, rho, pr, E, Rmass, Rmom, Rener, stream);
 }
@@ -294,6 +301,9 @@ int msod_diffusion_ijk(int porder, int nelem, int npoin, const int *connec, cons
                        float *Rener, void *stream)
 {
     (void)Ngp; (void)dNgp; (void)xgp;
+    if (!mode_is_default_diffusion())
+        return mode_diffusion(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
+                              gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs, Rmass, Rmom, Rener, stream);
     return diffu_impl<float>(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
                              gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs, Rmass, Rmom, Rener, stream);
 }

@@ -121,7 +121,8 @@ int msod_entropy_viscosity(int porder, int nelem, int npoin, const int *connec, 
     clear_error();
     int rc = geometry_ok(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK);
     if (rc) return rc;
-    if (!rho || !u || !pr || !mu_e) return set_error(MSOD_ERR_INVALID_ARG, "NULL field or mu_e");
+    if (!rho || !u || !pr || !(mu_e || nu_elem))
+        return set_error(MSOD_ERR_INVALID_ARG, "NULL field, or neither mu_e nor nu_elem");
     if (!(gamma > 1.0f)) return set_error(MSOD_ERR_INVALID_ARG, "gamma must exceed 1");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     EntropyStats *stats = nullptr;

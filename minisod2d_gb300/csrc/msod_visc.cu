@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(G::NT)
             continue;
         }
         const int o = el * ES + sLat[a];
-        mu_e[(size_t)a * nelem + ee] = sF[V_RHO * NPL + o] * nu;
+        if (mu_e) mu_e[(size_t)a * nelem + ee] = sF[V_RHO * NPL + o] * nu;
         if (a == 0) {
             if (nu_out) nu_out[ee] = nu;
             if (numax_out) numax_out[ee] = numax;

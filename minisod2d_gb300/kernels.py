@@ -179,6 +179,24 @@ def set_checked(enabled):
     capi.call("msod_set_checked", 1 if enabled else 0)
 
 
+def set_mode(precision="fp32", mu_e="given", mlp=None):
+    """The form of every later full_convec_ijk / full_diffusion_ijk call
+    (msod_set_mode): precision "fp32", "fp16" or "bf16"; mu_e "given",
+    "plain" (entropy-viscosity estimator) or "learned" (``mlp``, a learn.Mlp)."""
+    prec = {"fp32": capi.MSOD_PREC_FP32, "fp16": capi.MSOD_PREC_FP16, "bf16": capi.MSOD_PREC_BF16}[precision]
+    mue = {"given": capi.MSOD_MU_E_GIVEN, "plain": capi.MSOD_MU_E_PLAIN, "learned": capi.MSOD_MU_E_LEARNED}[mu_e]
+    capi.call("msod_set_mode", prec, mue, mlp.h if mlp is not None else None)
+
+
+def get_mode():
+    import ctypes as C
+
+    p, m = C.c_int(), C.c_int()
+    capi.call("msod_get_mode", C.byref(p), C.byref(m))
+    return ({capi.MSOD_PREC_FP32: "fp32", capi.MSOD_PREC_FP16: "fp16", capi.MSOD_PREC_BF16: "bf16"}[p.value],
+            {capi.MSOD_MU_E_GIVEN: "given", capi.MSOD_MU_E_PLAIN: "plain", capi.MSOD_MU_E_LEARNED: "learned"}[m.value])
+
+
 __all__ = ["full_convec_ijk", "full_convec_ijk_split", "full_diffusion_ijk", "full_convec_ijk_mixed",
-           "full_diffusion_ijk_mixed", "elem_jacobian",
+           "full_diffusion_ijk_mixed", "elem_jacobian", "set_mode", "get_mode",
            "check_element_tables", "set_checked"]

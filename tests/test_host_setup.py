@@ -135,3 +135,24 @@ def test_no_device_is_reported(msod_lib):
         pytest.skip("a device is present")
     rc = capi.lib().msod_init(0)
     assert rc == capi.MSOD_ERR_NO_DEVICE
+
+
+def test_mode_switch_arguments():
+    """msod_set_mode: round trip through msod_get_mode, rejected values, back to the default."""
+    from minisod2d_gb300 import capi, kernels
+
+    try:
+        assert kernels.get_mode() == ("fp32", "given")
+        kernels.set_mode("fp16", "plain")
+        assert kernels.get_mode() == ("fp16", "plain")
+        with pytest.raises(capi.MsodError) as ei:
+            capi.call("msod_set_mode", 7, 0, None)
+        assert ei.value.code == capi.MSOD_ERR_INVALID_ARG
+        with pytest.raises(capi.MsodError):
+            capi.call("msod_set_mode", capi.MSOD_PREC_FP32, 9, None)
+        with pytest.raises(capi.MsodError):  # the learned mode needs a network
+            capi.call("msod_set_mode", capi.MSOD_PREC_FP32, capi.MSOD_MU_E_LEARNED, None)
+        assert kernels.get_mode() == ("fp16", "plain")  # a rejected call changes nothing
+    finally:
+        kernels.set_mode()
+    assert kernels.get_mode() == ("fp32", "given")
