@@ -13,11 +13,14 @@
 //   the output node (elem_diffu.f90:143-146).
 //
 // Design (persistent blocks, groups of NE elements, one thread per GLL line):
-//   0. node ids of group g+2 are loaded into registers and the node fields
-//      (rho, T, u, mu_fluid) plus the element-layout mu_e, mu_sgs of group g+1
-//      are gathered with cp.async into the other half of a double-buffered
-//      shared-memory lattice while group g is computed; the He and gpvol
-//      values of the point pass are loaded into registers before pass 1;
+//   0. the node ids of the next group are loaded into registers while the
+//      current group is computed; after it, the next group's node fields
+//      (rho, T, u, mu_fluid) and element-layout mu_e, mu_sgs are gathered with
+//      cp.async into the shared-memory lattice (single-buffered: measured 6 %
+//      faster than a double-buffered lattice, whose shared memory held the
+//      kernel to two blocks per SM instead of three; DIFFU_NBUF = 2 selects
+//      it); the He and gpvol values of the point pass are loaded into
+//      registers before pass 1;
 //   1. three line passes store the 15 iso-parametric derivatives per point;
 //   2. a point pass turns them into physical gradients and stress and stores,
 //      per direction d, the contravariant fluxes gpvol * He(:,d)^T X for the
@@ -32,6 +35,13 @@
 #include "msod_device.cuh"
 #include "msod_kernels.h"
 #include "msod_mlp.cuh"
+
+// Lattices of gathered node fields: 2 = double-buffered (the next group's
+// fields are gathered with cp.async while the current group is computed),
+// 1 = single (less shared memory, more blocks per SM).
+#ifndef DIFFU_NBUF
+#define DIFFU_NBUF 1
+#endif
 
 namespace msod {
 namespace {
@@ -142,7 +152,8 @@ __device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::re
 template <class G>
 constexpr size_t diffu_smem_bytes()
 {
-    return (size_t)(2 * NDF + 3 * NX) * G::NPL * sizeof(typename G::real) + (size_t)(2 * G::NPL + 2 * G::N) * sizeof(int);
+    return (size_t)(DIFFU_NBUF * NDF + 3 * NX) * G::NPL * sizeof(typename G::real) +
+           (size_t)(DIFFU_NBUF * G::NPL + 2 * G::N) * sizeof(int);
 }
 
 template <typename real, int P>
@@ -179,10 +190,11 @@ __global__ void __launch_bounds__(G::NT)
     constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT, NPL = G::NPL;
     constexpr int IPT = (NE * N + NT - 1) / NT;  // items (node ids, points) per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    real *sF = reinterpret_cast<real *>(smem_raw);  // [2][NDF][NPL]
-    real *sX = sF + 2 * NDF * NPL;                   // [3*NX][NPL]
-    int *sNode = reinterpret_cast<int *>(sX + 3 * NX * NPL);  // [2][NPL]
-    int *sPerm = sNode + 2 * NPL;
+    constexpr int NBUF = DIFFU_NBUF;
+    real *sF = reinterpret_cast<real *>(smem_raw);  // [NBUF][NDF][NPL]
+    real *sX = sF + NBUF * NDF * NPL;                // [3*NX][NPL]
+    int *sNode = reinterpret_cast<int *>(sX + 3 * NX * NPL);  // [NBUF][NPL]
+    int *sPerm = sNode + NBUF * NPL;
     int *sLat = sPerm + N;
     float *sNet = reinterpret_cast<float *>(sLat + N);  // network mode: weights, then per-group data
     float *sFeat = sNet + kNetWords;                      // [NE][12]
@@ -363,18 +375,20 @@ __global__ void __launch_bounds__(G::NT)
     const LineThread<G> lt(tid);
     const real twoThirds = (real)2 / (real)3;
     int s = 0;
-    for (; g < ngroups; g = gn, gn += stride, s ^= 1) {
+    for (; g < ngroups; g = gn, gn += stride, s = NBUF == 2 ? s ^ 1 : 0) {
         real *sFs = sF + s * NDF * NPL;
         int *sNs = sNode + s * NPL;
         real Hm[IPT][9], gv[IPT];
         load_metric(g, Hm, gv);
-        if (gn < ngroups) store_ids(ids, sNode + (s ^ 1) * NPL);
+        if (NBUF == 2 && gn < ngroups) store_ids(ids, sNode + (s ^ 1) * NPL);
         store_net();
         cp_async_wait_all();
         __syncthreads();
         if (gn < ngroups) {
-            gather(gn, sNode + (s ^ 1) * NPL, sF + (s ^ 1) * NDF * NPL);
-            if (gn + stride < ngroups) load_ids(gn + stride, ids);
+            if (NBUF == 2) {
+                gather(gn, sNode + (s ^ 1) * NPL, sF + (s ^ 1) * NDF * NPL);
+                if (gn + stride < ngroups) load_ids(gn + stride, ids);
+            }
             load_net(gn);
         }
         run_net(g);
@@ -443,6 +457,12 @@ __global__ void __launch_bounds__(G::NT)
         __syncthreads();
         if (lt.active) div_pass<G, 2>(lt, sFs, sX, sNs, npoin, Rmass, Rmom, Rener);
         __syncthreads();
+        if (NBUF == 1 && gn < ngroups) {  // the next group's node ids, then its fields
+            store_ids(ids, sNode);
+            __syncthreads();
+            gather(gn, sNode, sF);
+            if (gn + stride < ngroups) load_ids(gn + stride, ids);
+        }
     }
 }
 
