@@ -18,8 +18,10 @@
 // faster than a persistent, cp.async double-buffered variant of the same
 // passes: the kernel is bound by FP32 issue and He-load latency, not by the
 // gathers):
-//   * the block reads the 1-D derivative matrices and node permutations from
-//     the caller's dlxigp_ip / invAtoIJK / gmshAtoI/J/K into shared memory;
+//   * the block copies the node permutations of the call's tables (prepared
+//     once per call from the caller's invAtoIJK / gmshAtoI/J/K, msod_tables.cu)
+//     into shared memory while its connec entries load; the 1-D derivative
+//     matrices are constant-bank operands (shared memory when S > 1);
 //   * connec is read coalesced along elements (it is element-fastest), node
 //     fields are gathered into a per-element (I,J,K) lattice in shared memory;
 //   * each thread owns one GLL line (S threads share a line at high order).
@@ -286,7 +288,8 @@ __global__ void __launch_bounds__(LineGeom<real, P>::NT, convec_minb<real, P>())
                   const int *__restrict__ invAtoIJK, const int *__restrict__ AtoI,
                   const int *__restrict__ AtoJ, const int *__restrict__ AtoK, const real *__restrict__ u,
                   const real *__restrict__ q, const real *__restrict__ rho, const real *__restrict__ pr,
-                  const real *__restrict__ E, real *__restrict__ Rmass, real *__restrict__ Rmom,
+                  const real *__restrict__ E, const TableScratch *__restrict__ tabs, real *__restrict__ Rmass,
+                  real *__restrict__ Rmom,
                   real *__restrict__ Rener)
 {
     using G = LineGeom<real, P>;
@@ -302,17 +305,30 @@ __global__ void __launch_bounds__(LineGeom<real, P>::NT, convec_minb<real, P>())
 
     const int tid = threadIdx.x;
     const int e0 = blockIdx.x * NE;
-    load_element_tables<real, P>(invAtoIJK, AtoI, AtoJ, AtoK, dlxigp_ip, sPerm, sLat, sD, tid, NT);
-
-    // Node ids of the group's elements; connec is element-fastest.
-    for (int i = tid; i < NE * N; i += NT) {
+    // Node ids of the group's elements (connec is element-fastest), loaded
+    // while the per-call tables are copied into shared memory.
+    constexpr int IPT = (NE * N + NT - 1) / NT;
+    int ids[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = tid + k * NT;
         const int el = i % NE, a = i / NE, e = e0 + el;
-        int node = -1;
-        if (e < nelem) {
-            const int v = ldg(connec + (size_t)a * nelem + e) - 1;
-            node = (v >= 0 && v < npoin) ? v : -1;
+        ids[k] = (i < NE * N && e < nelem) ? ldg(connec + (size_t)a * nelem + e) - 1 : -1;
+    }
+    for (int i = tid; i < N; i += NT) {
+        sPerm[i] = tabs->perm[i];
+        sLat[i] = tabs->lat[i];
+    }
+    if (G::S > 1)
+        for (int i = tid; i < 3 * Q * Q; i += NT) sD[i] = table_D<real>(tabs)[i];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = tid + k * NT;
+        if (i < NE * N) {
+            const int v = ids[k];
+            sNode[(i % NE) * ES + sLat[i / NE]] = (v >= 0 && v < npoin) ? v : -1;
         }
-        sNode[el * ES + sLat[a]] = node;
     }
     __syncthreads();
     // Gather node fields into the lattice.
@@ -363,8 +379,8 @@ cudaError_t launch_convec_p(const ConvecArgs<real> &a, const TableScratch *tabs,
     static_assert(smem <= 227 * 1024, "shared memory budget");
     cudaError_t err = cudaFuncSetAttribute(convec_kernel<real, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
+    if (!tabs) return cudaErrorInvalidValue;
     if (G::S == 1) {
-        if (!tabs) return cudaErrorInvalidValue;
         if (sizeof(real) == 4)
             err = cudaMemcpyToSymbolAsync(c_CDf, table_D<float>(tabs), sizeof(float) * 3 * G::Q * G::Q,
                                           sizeof(float) * kTableDMax * P, cudaMemcpyDeviceToDevice, st);
@@ -376,7 +392,7 @@ cudaError_t launch_convec_p(const ConvecArgs<real> &a, const TableScratch *tabs,
     const unsigned grid = (unsigned)((a.nelem + G::NE - 1) / G::NE);
     convec_kernel<real, P><<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.dlxigp_ip,
                                                       a.invAtoIJK, a.AtoI, a.AtoJ, a.AtoK, a.u, a.q, a.rho,
-                                                      a.pr, a.E, a.Rmass, a.Rmom, a.Rener);
+                                                      a.pr, a.E, tabs, a.Rmass, a.Rmom, a.Rener);
     return cudaGetLastError();
 }
 
