@@ -331,30 +331,27 @@ __global__ void __launch_bounds__(LineGeom<real, P>::NT, convec_minb<real, P>())
         }
     }
     __syncthreads();
-    // Gather node fields into the lattice.
+    // Gather node fields into the lattice: asynchronous copies, all of a
+    // thread's in flight at once (a missing node reads as zeros).
     const size_t np = (size_t)npoin;
     for (int i = tid; i < NE * N; i += NT) {
         const int el = i / N, l = i - el * N;
         const int I = l % Q, J = (l / Q) % Q, K = l / (Q * Q);
         const int o = el * ES + (K * Q + J) * QP + I;
         const int p = sNode[o];
-        real v[NFIELD];
-        if (p >= 0) {
-            v[F_RHO] = ldg(rho + p);
-            v[F_P] = ldg(pr + p);
-            v[F_E] = ldg(E + p);
+        const bool ok = p >= 0;
+        const size_t pp = ok ? (size_t)p : 0;
+        cp_async_elem(sF + F_RHO * NPL + o, rho + pp, ok);
+        cp_async_elem(sF + F_P * NPL + o, pr + pp, ok);
+        cp_async_elem(sF + F_E * NPL + o, E + pp, ok);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                v[F_U0 + c] = ldg(u + c * np + p);
-                v[F_Q0 + c] = ldg(q + c * np + p);
-            }
-        } else {
-#pragma unroll
-            for (int c = 0; c < NFIELD; ++c) v[c] = (real)0;
+        for (int c = 0; c < 3; ++c) {
+            cp_async_elem(sF + (F_U0 + c) * NPL + o, u + c * np + pp, ok);
+            cp_async_elem(sF + (F_Q0 + c) * NPL + o, q + c * np + pp, ok);
         }
-#pragma unroll
-        for (int c = 0; c < NFIELD; ++c) sF[c * NPL + o] = v[c];
     }
+    cp_async_commit();
+    cp_async_wait_all();
     __syncthreads();
     convec_pass<real, P, 0>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
     __syncthreads();
