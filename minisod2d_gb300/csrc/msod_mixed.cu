@@ -214,15 +214,18 @@ __global__ void __launch_bounds__(kThreads)
         const bool ok = (unsigned)v < (unsigned)npoin;
         const int p = ok ? v : 0;
         sNode[l] = ok ? v : -1;
-        sBase[B_RHO * N + l] = ok ? ldg(rho + p) : 0.0f;
-        sBase[B_P * N + l] = ok ? ldg(pr + p) : 0.0f;
-        sBase[B_E * N + l] = ok ? ldg(E + p) : 0.0f;
+        // asynchronous copies (a missing node reads as zeros)
+        cp_async_elem(sBase + B_RHO * N + l, rho + p, ok);
+        cp_async_elem(sBase + B_P * N + l, pr + p, ok);
+        cp_async_elem(sBase + B_E * N + l, E + p, ok);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            sBase[(B_U0 + c) * N + l] = ok ? ldg(u + c * np + p) : 0.0f;
-            sBase[(B_Q0 + c) * N + l] = ok ? ldg(q + c * np + p) : 0.0f;
+            cp_async_elem(sBase + (B_U0 + c) * N + l, u + c * np + p, ok);
+            cp_async_elem(sBase + (B_Q0 + c) * N + l, q + c * np + p, ok);
         }
     }
+    cp_async_commit();
+    cp_async_wait_all();
     __syncthreads();
 
     // He columns of the first direction pass, in flight during the split.

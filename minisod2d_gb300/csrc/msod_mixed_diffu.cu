@@ -144,15 +144,20 @@ __global__ void __launch_bounds__(kThreads)
             const bool ok = (unsigned)v < (unsigned)npoin;
             const int p = ok ? v : 0;
             sNode[l] = ok ? v : -1;
-            const float r = ok ? ldg(rho + p) : 1.0f;
+            const float r = ok ? ldg(rho + p) : 1.0f;  // 1 at a missing node keeps nu_e = mu_e / rho finite
             sB[S_RHO * N + l] = r;
-            sB[S_T * N + l] = ok ? ldg(Tem + p) : 0.0f;
+            // the other fields by asynchronous copies (a missing node reads as zeros)
+            cp_async_elem(sB + S_T * N + l, Tem + p, ok);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) sB[(S_U0 + c) * N + l] = ok ? ldg(u + c * np + p) : 0.0f;
-            sB[S_MUF * N + l] = ok ? ldg(mu_fluid + p) : 0.0f;
-            sB[S_MUE * N + l] = NUE ? r * nue : ldg(mu_e + (size_t)a * nelem + e);
-            sB[S_MUS * N + l] = ldg(mu_sgs + (size_t)a * nelem + e);
+            for (int c = 0; c < 3; ++c) cp_async_elem(sB + (S_U0 + c) * N + l, u + c * np + p, ok);
+            cp_async_elem(sB + S_MUF * N + l, mu_fluid + p, ok);
+            if (NUE)
+                sB[S_MUE * N + l] = r * nue;
+            else
+                cp_async_elem(sB + S_MUE * N + l, mu_e + (size_t)a * nelem + e, true);
+            cp_async_elem(sB + S_MUS * N + l, mu_sgs + (size_t)a * nelem + e, true);
         }
+        cp_async_commit();
         // He and gpvol of the point-pass points, in flight during the gradient stage.
         float hv[TPT][2][9], gv[TPT][2];
 #pragma unroll
@@ -168,6 +173,7 @@ __global__ void __launch_bounds__(kThreads)
                 gv[tk][h] = ldg(gpvol + base);
             }
         }
+        cp_async_wait_all();
         __syncthreads();
 
         // ---- gradient stage: split rho, T, u_1..3 (shifted by node (0,0,0)) ----
