@@ -62,21 +62,40 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
                     int *__restrict__ flag)
 {
     constexpr int Q = P + 1, N = Q * Q * Q, kFeatWarps = feat_warps<P>();
+    constexpr int NPL = (N + 31) / 32;  // nodes per lane
     __shared__ float sv[kFeatWarps][5][N];  // rho, p, u0, u1, u2 by gmsh node
+    __shared__ int sPerm[N];                // lattice -> gmsh node
+    __shared__ float sD[3 * Q * Q];         // 1-D derivative matrices
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int e = blockIdx.x * kFeatWarps + w;
-    if (e >= nelem) return;
     const TableScratch *t = tabs;
+    for (int i = threadIdx.x; i < N; i += 32 * kFeatWarps) sPerm[i] = t->perm[i];
+    for (int i = threadIdx.x; i < 3 * Q * Q; i += 32 * kFeatWarps) sD[i] = t->Df[i];
+    __syncthreads();
+    if (e >= nelem) return;
+    // Entropy normalisation (read early: its latency hides behind the gathers).
+    const double esum = st->sum;
+    const int ekmin = st->kmin, ekmax = st->kmax;
     float rmin = 3e38f, rmax = -3e38f, rsum = 0.f, pmin = 3e38f, pmax = -3e38f, psum = 0.f;
     float smin = 3e38f, smax = -3e38f, emin = 3e38f, emax = -3e38f, machmax = 0.f, usum = 0.f, csum = 0.f;
     float spdmax = 0.f, vol = 0.f;
     const size_t np = (size_t)npoin;
-    for (int a = lane; a < N; a += 32) {
-        int p = ldg(connec + (size_t)a * nelem + e) - 1;
-        p = min(max(p, 0), npoin - 1);
+    // All of the lane's node ids first, then its field loads, so that the loads overlap.
+    int pn[NPL];
+#pragma unroll
+    for (int k = 0; k < NPL; ++k) {
+        const int a = lane + 32 * k;
+        pn[k] = a < N ? min(max(ldg(connec + (size_t)a * nelem + e) - 1, 0), npoin - 1) : 0;
+    }
+#pragma unroll 4
+    for (int k = 0; k < NPL; ++k) {
+        const int a = lane + 32 * k;
+        if (a >= N) break;
+        const int p = pn[k];
         const float r = ldg(rho + p);
         const float pr = Rgas > 0.0f ? r * Rgas * ldg(p_or_T + p) : ldg(p_or_T + p);
         const float ux = ldg(u + p), uy = ldg(u + np + p), uz = ldg(u + 2 * np + p);
+        vol += ldg(gpvol + (size_t)e * N + a);
         sv[w][0][a] = r;
         sv[w][1][a] = pr;
         sv[w][2][a] = ux;
@@ -91,7 +110,6 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
         machmax = fmaxf(machmax, um / c);
         usum += um; csum += c;
         spdmax = fmaxf(spdmax, um + c);
-        vol += ldg(gpvol + (size_t)e * N + a);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -106,21 +124,25 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
         vol += __shfl_xor_sync(~0u, vol, o);
     }
     __syncwarp();
-    if (lane != 0) return;
-    double mean = st->sum / (double)npoin;
-    double lo = (double)key2f(st->kmin), hi = (double)key2f(st->kmax);
-    float neta = (float)fmax(hi - mean, mean - lo);
-    if (!(neta > 0.0f)) neta = 1.0f;
-    const float rmean = rsum / N, pmean = psum / N, umean = usum / N, cmean = csum / N;
-    const float h = cbrtf(vol) / (float)P;
     // Centre node and the natural -> SOD 1-D index map (0 -> 0, P -> 1, k -> k+1).
     const int mnat = P / 2;
     const int ms = mnat == 0 ? 0 : (mnat == P ? 1 : mnat + 1);
-    auto node = [&](int I, int J, int K) { return t->perm[(K * Q + J) * Q + I]; };
+    auto node = [&](int I, int J, int K) { return sPerm[(K * Q + J) * Q + I]; };
     const int nat[3] = {0, ms, 1};  // SOD positions of natural 0, mid, P
-    float d2r = 0.f, d2e = 0.f, defect = 0.f;
-    float gi[3][3];  // iso derivative of u_i along d at the centre
-    for (int d = 0; d < 3; ++d) {
+    // Lanes 0-8: iso derivative gi[i][d] of u_i along d at the centre (lane 3i + d);
+    // lanes 9-11: second differences and product-rule defect along d = lane - 9;
+    // lanes 12-20: He at the centre node.
+    float gval = 0.f, d2r_l = 0.f, d2e_l = 0.f, def_l = 0.f, hval = 0.f;
+    if (lane < 9) {
+        const int i = lane / 3, d = lane % 3;
+        float sacc = 0.f;
+        for (int c = 0; c < Q; ++c) {
+            const int I = d == 0 ? c : ms, J = d == 1 ? c : ms, K = d == 2 ? c : ms;
+            sacc = fmaf(sD[(d * Q + ms) * Q + c], sv[w][2 + i][node(I, J, K)], sacc);
+        }
+        gval = sacc;
+    } else if (lane < 12) {
+        const int d = lane - 9;
         float rv[3], ev[3], uv[3];
         for (int k = 0; k < 3; ++k) {
             const int I = d == 0 ? nat[k] : ms, J = d == 1 ? nat[k] : ms, K = d == 2 ? nat[k] : ms;
@@ -130,24 +152,37 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
             ev[k] = r * (logf(pr) - gamma * logf(r)) / (gamma - 1.0f);
             uv[k] = sv[w][2 + d][a];
         }
-        d2r = fmaxf(d2r, fabsf(rv[0] - 2.f * rv[1] + rv[2]));
-        d2e = fmaxf(d2e, fabsf(ev[0] - 2.f * ev[1] + ev[2]));
+        d2r_l = fabsf(rv[0] - 2.f * rv[1] + rv[2]);
+        d2e_l = fabsf(ev[0] - 2.f * ev[1] + ev[2]);
         const float A = ev[2] * uv[2] - ev[0] * uv[0];
         const float B = ev[1] * (uv[2] - uv[0]) + uv[1] * (ev[2] - ev[0]);
-        defect = fmaxf(defect, fabsf(A - B));
-        for (int i = 0; i < 3; ++i) {
-            float s = 0.f;
-            for (int c = 0; c < Q; ++c) {
-                const int I = d == 0 ? c : ms, J = d == 1 ? c : ms, K = d == 2 ? c : ms;
-                s = fmaf(t->Df[(d * Q + ms) * Q + c], sv[w][2 + i][node(I, J, K)], s);
-            }
-            gi[i][d] = s;
-        }
+        def_l = fabsf(A - B);
+    } else if (lane < 21) {
+        hval = ldg(He + ((size_t)e * N + node(ms, ms, ms)) * 9 + (lane - 12));
     }
-    const float *hp = He + ((size_t)e * N + node(ms, ms, ms)) * 9;
+    float gi[3][3], Hc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        gi[k / 3][k % 3] = __shfl_sync(~0u, gval, k);
+        Hc[k] = __shfl_sync(~0u, hval, 12 + k);
+    }
+    float d2r = 0.f, d2e = 0.f, defect = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        d2r = fmaxf(d2r, __shfl_sync(~0u, d2r_l, 9 + d));
+        d2e = fmaxf(d2e, __shfl_sync(~0u, d2e_l, 9 + d));
+        defect = fmaxf(defect, __shfl_sync(~0u, def_l, 9 + d));
+    }
+    if (lane != 0) return;
+    const double mean = esum / (double)npoin;
+    const double lo = (double)key2f(ekmin), hi = (double)key2f(ekmax);
+    float neta = (float)fmax(hi - mean, mean - lo);
+    if (!(neta > 0.0f)) neta = 1.0f;
+    const float rmean = rsum / N, pmean = psum / N, umean = usum / N, cmean = csum / N;
+    const float h = cbrtf(vol) / (float)P;
     float G[3][3];  // G[i][j] = d u_i / d x_j = sum_k He(j,k) gi[i][k]
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) G[i][j] = ldg(hp + 0 * 3 + j) * gi[i][0] + ldg(hp + 3 + j) * gi[i][1] + ldg(hp + 6 + j) * gi[i][2];
+        for (int j = 0; j < 3; ++j) G[i][j] = Hc[0 * 3 + j] * gi[i][0] + Hc[3 + j] * gi[i][1] + Hc[6 + j] * gi[i][2];
     const float theta = G[0][0] + G[1][1] + G[2][2];
     const float w0 = G[2][1] - G[1][2], w1 = G[0][2] - G[2][0], w2 = G[1][0] - G[0][1];
     float s2 = 0.f;
