@@ -70,6 +70,7 @@ __global__ void entropy_stats_kernel(int npoin, const float *__restrict__ rho, c
 // Plain estimator: one group of NE elements per block, one thread per line.
 // ---------------------------------------------------------------------------
 enum { V_RHO = 0, V_P, V_U0, V_U1, V_U2, NVF };
+constexpr int V_ETA = V_P;  // after the per-point preparation the pressure plane holds eta
 
 template <class G, int DIR>
 __device__ __forceinline__ void residual_pass(const LineThread<G> &lt, const float *__restrict__ sF,
@@ -80,14 +81,16 @@ __device__ __forceinline__ void residual_pass(const LineThread<G> &lt, const flo
     constexpr int Q = G::Q, QP = G::QP, R = G::R, NPL = G::NPL;
     constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
     const int base = lt.el * G::ES + line_off<DIR, Q, QP>(lt.la, lt.lb, 0);
-    float eta[Q], u_[3][Q];
+    float eta[Q], u_[3][Q], eu[3][Q];
 #pragma unroll
     for (int c = 0; c < Q; ++c) {
         const int o = base + c * OST;
-        const float r = sF[V_RHO * NPL + o], p = sF[V_P * NPL + o];
-        eta[c] = r / (gamma - 1.0f) * (logf(p) - gamma * logf(r));
+        eta[c] = sF[V_ETA * NPL + o];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) u_[i][c] = sF[(V_U0 + i) * NPL + o];
+        for (int i = 0; i < 3; ++i) {
+            u_[i][c] = sF[(V_U0 + i) * NPL + o];
+            eu[i][c] = eta[c] * u_[i][c];
+        }
     }
 #pragma unroll
     for (int rr = 0; rr < R; ++rr) {
@@ -98,17 +101,19 @@ __device__ __forceinline__ void residual_pass(const LineThread<G> &lt, const flo
         const float h0 = ldg(hp), h1 = ldg(hp + 1), h2 = ldg(hp + 2);
         const float hh[3] = {h0, h1, h2};
         float deta = 0.0f, ddiv = 0.0f, dveta = 0.0f;  // D.eta, sum_i h_i D.(eta u_i), sum_i h_i D.u_i
-        float dv[3] = {0.0f, 0.0f, 0.0f};
+        float dv[3] = {0.0f, 0.0f, 0.0f}, deu[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
         for (int c = 0; c < Q; ++c) {
             const float d = sD[(DIR * Q + r) * Q + c];
             deta = fmaf(d, eta[c], deta);
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-                ddiv = fmaf(d * hh[i], eta[c] * u_[i][c], ddiv);
+                deu[i] = fmaf(d, eu[i][c], deu[i]);
                 dv[i] = fmaf(d, u_[i][c], dv[i]);
             }
         }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) ddiv = fmaf(hh[i], deu[i], ddiv);
         float own_eta = eta[0], own_u[3] = {u_[0][0], u_[1][0], u_[2][0]};
 #pragma unroll
         for (int c = 1; c < Q; ++c)
@@ -188,8 +193,38 @@ __global__ void __launch_bounds__(G::NT)
 #pragma unroll
             for (int c = 0; c < 3; ++c) v[V_U0 + c] = ldg(u + c * np + p);
         }
+        // Per point once: the entropy (replacing the pressure), the element
+        // maxima of |u| + c and the element volume.
+        const float spd = sqrtf(v[V_U0] * v[V_U0] + v[V_U1] * v[V_U1] + v[V_U2] * v[V_U2]) +
+                          sqrtf(gamma * v[V_P] / v[V_RHO]);
+        v[V_ETA] = v[V_RHO] / (gamma - 1.0f) * (logf(v[V_P]) - gamma * logf(v[V_RHO]));
 #pragma unroll
         for (int c = 0; c < NVF; ++c) sF[c * NPL + o] = v[c];
+        sR[o] = spd;  // the residual plane is free until the first pass
+    }
+    __syncthreads();
+    // One warp per element: max |u| + c and the volume (warp reductions, no
+    // shared-memory atomics on one address per element).
+    {
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int el = warp; el < NE; el += NT / 32) {
+            const int ee = e0 + el;
+            unsigned mx = 0u;
+            float vol = 0.0f;
+            if (ee < nelem)
+                for (int l = lane; l < N; l += 32) {
+                    const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
+                    mx = max(mx, __float_as_uint(sR[o]));  // non-negative floats order like their bits
+                    vol += ldg(gpvol + (size_t)ee * N + sPerm[l]);
+                }
+            mx = __reduce_max_sync(0xffffffffu, mx);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) vol += __shfl_xor_sync(0xffffffffu, vol, off);
+            if (lane == 0) {
+                s_kS[el] = (int)mx;
+                s_vol[el] = vol;
+            }
+        }
     }
     __syncthreads();
     const LineThread<G> lt(tid);
@@ -201,17 +236,19 @@ __global__ void __launch_bounds__(G::NT)
     __syncthreads();
     if (live) residual_pass<G, 2>(lt, sF, sR, sPerm, sD, He, e, gamma);
     __syncthreads();
-    // Element maxima of |R| and |u| + c, element volume.
-    for (int i = tid; i < NE * N; i += NT) {
-        const int el = i / N, l = i - el * N, ee = e0 + el;
-        if (ee >= nelem) continue;
-        const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
-        const float r = sF[V_RHO * NPL + o], p = sF[V_P * NPL + o];
-        const float ux = sF[V_U0 * NPL + o], uy = sF[V_U1 * NPL + o], uz = sF[V_U2 * NPL + o];
-        const float spd = sqrtf(ux * ux + uy * uy + uz * uz) + sqrtf(gamma * p / r);
-        atomicMax(&s_kR[el], __float_as_int(fabsf(sR[o])));
-        atomicMax(&s_kS[el], __float_as_int(spd));
-        atomicAdd(&s_vol[el], ldg(gpvol + (size_t)ee * N + sPerm[l]));
+    // Element maxima of |R| (one warp per element).
+    {
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int el = warp; el < NE; el += NT / 32) {
+            unsigned mx = 0u;
+            if (e0 + el < nelem)
+                for (int l = lane; l < N; l += 32) {
+                    const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
+                    mx = max(mx, __float_as_uint(fabsf(sR[o])));
+                }
+            mx = __reduce_max_sync(0xffffffffu, mx);
+            if (lane == 0) s_kR[el] = (int)mx;
+        }
     }
     __syncthreads();
     float neta = 1.0f;
