@@ -53,16 +53,39 @@ __global__ void entropy_stats_kernel(int npoin, const float *__restrict__ rho, c
         mn = fminf(mn, eta);
         mx = fmaxf(mx, eta);
     }
+    // Warp, then block reduction: one set of global atomics per block (the
+    // atomics on these three words serialise in L2).
+    double sd = (double)s;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        s += __shfl_xor_sync(0xffffffffu, s, o);
+        sd += __shfl_xor_sync(0xffffffffu, sd, o);
         mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&st->sum, (double)s);
-        atomicMin(&st->kmin, f2key(mn));
-        atomicMax(&st->kmax, f2key(mx));
+    __shared__ double bs[32];
+    __shared__ float bmn[32], bmx[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+        bs[warp] = sd;
+        bmn[warp] = mn;
+        bmx[warp] = mx;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        sd = lane < nw ? bs[lane] : 0.0;
+        mn = lane < nw ? bmn[lane] : 3.0e38f;
+        mx = lane < nw ? bmx[lane] : -3.0e38f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sd += __shfl_xor_sync(0xffffffffu, sd, o);
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if (lane == 0) {
+            atomicAdd(&st->sum, sd);
+            atomicMin(&st->kmin, f2key(mn));
+            atomicMax(&st->kmax, f2key(mx));
+        }
     }
 }
 
@@ -306,8 +329,10 @@ cudaError_t launch_entropy_stats(int npoin, const float *rho, const float *p_or_
     entropy_stats_init<<<1, 1, 0, s>>>(st);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int blocks = (npoin + 255) / 256;
-    if (blocks > 4096) blocks = 4096;
+    if (blocks > 8 * sms) blocks = 8 * sms;
     entropy_stats_kernel<<<blocks, 256, 0, s>>>(npoin, rho, p_or_T, Rgas, gamma, st);
     return cudaGetLastError();
 }
