@@ -58,6 +58,8 @@ def build(force=False, verbose=False, ptxas_verbose=False):
     for f in cu:
         obj = os.path.join(BUILD, f + ".o")
         extra = ["-Xptxas", "-v"] if ptxas_verbose else []
+        # Compile-time kernel variants (e.g. -DCONVEC_MINB=3), for measuring.
+        extra += os.environ.get("MSOD_NVCC_DEFINES", "").split()
         jobs.append(([_nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, f), "-o", obj], f))
         objs.append(obj)
     for f in cpp:

@@ -41,6 +41,13 @@
 #ifndef CONVEC_MINB
 #define CONVEC_MINB 4
 #endif
+#ifndef CONVEC_MINB5
+#define CONVEC_MINB5 3
+#endif
+// Blocks per SM for the 256-thread blocks of porder 5.
+#ifndef CONVEC_MINB_WIDE
+#define CONVEC_MINB_WIDE 1
+#endif
 
 namespace msod {
 namespace {
@@ -64,6 +71,26 @@ __device__ __forceinline__ double cCD<double>(int P, int i)
     return c_CDd[P][i];
 }
 
+// Elements per block at porder 5 in FP32 (36 threads per element): 3 fill a
+// 128-thread block (with the packed passes at three blocks per SM: 3.05 ms
+// against 3.62 ms for seven elements in a 256-thread block at one block per
+// SM, 64^3 hexes).
+#ifndef CONVEC_NE5
+#define CONVEC_NE5 3
+#endif
+template <typename real, int P>
+using ConvecGeom = LineGeom<real, P, (sizeof(real) == 4 && P == 5) ? CONVEC_NE5 : 64>;
+
+// Row pairs of the FP32 matrices (packed contractions), per porder:
+// c_CDp[P][(d*Q + c)*H + m] = (D[d][2m][c], D[d][2m+1][c]), H = (Q+1)/2.
+__constant__ float2 c_CDp[MSOD_MAX_PORDER + 1][kTableDPairMax / 2];
+
+// Packed (f32x2) line passes: 0 never, 1 at porder 5, 2 whenever FP32 runs
+// one thread per line.
+#ifndef CONVEC_X2
+#define CONVEC_X2 1
+#endif
+
 template <int Q, typename real>
 __device__ __forceinline__ real pick(const real (&a)[Q], int i)
 {
@@ -84,7 +111,7 @@ __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *_
                                             real *__restrict__ Rmass, real *__restrict__ Rmom,
                                             real *__restrict__ Rener)
 {
-    using G = LineGeom<real, P>;
+    using G = ConvecGeom<real, P>;
     constexpr int Q = G::Q, QP = G::QP, ES = G::ES, NE = G::NE, S = G::S, R = G::R, TPE = G::TPE, N = G::N;
     constexpr int NPL = NE * ES;
     constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
@@ -272,17 +299,243 @@ __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *_
     }
 }
 
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// The pass above for FP32 with one thread per line, two points of the line
+// per instruction: rows (2m, 2m+1) are the two halves of fma.rn.f32x2 /
+// mul.rn.f32x2 operands, operation for operation the scalar pass (a line of
+// odd length pads its last pair with a zero row that is never stored).
+template <int P, int DIR>
+__device__ __forceinline__ void convec_pass_x2(const float *__restrict__ sF, float *__restrict__ sA,
+                                               const int *__restrict__ sNode, const int *__restrict__ sPerm,
+                                               const float *__restrict__ He, const float *__restrict__ gpvol, int e0,
+                                               int nelem, int npoin, float *__restrict__ Rmass,
+                                               float *__restrict__ Rmom, float *__restrict__ Rener)
+{
+    using G = ConvecGeom<float, P>;
+    constexpr int Q = G::Q, QP = G::QP, ES = G::ES, NE = G::NE, TPE = G::TPE, N = G::N;
+    constexpr int H = (Q + 1) / 2;
+    constexpr int NPL = NE * ES;
+    constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
+    static_assert(G::S == 1, "one thread per line");
+
+    const int tid = threadIdx.x;
+    if (tid >= NE * TPE) return;
+    const int el = tid / TPE, line = tid - el * TPE;
+    const int la = line % Q, lb = line / Q;
+    const int e = e0 + el;
+    const int base = el * ES + line_off<DIR, Q, QP>(la, lb, 0);
+
+    float rho_[Q], p_[Q], H_[Q], rH_[Q], u_[3][Q], q_[3][Q];
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        const int o = base + c * OST;
+        rho_[c] = sF[F_RHO * NPL + o];
+        p_[c] = sF[F_P * NPL + o];
+        const float Ev = sF[F_E * NPL + o];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            u_[i][c] = sF[(F_U0 + i) * NPL + o];
+            q_[i][c] = sF[(F_Q0 + i) * NPL + o];
+        }
+        const float k = 0.5f * (u_[0][c] * u_[0][c] + u_[1][c] * u_[1][c] + u_[2][c] * u_[2][c]);
+        H_[c] = Ev + k;
+        rH_[c] = rho_[c] * H_[c];
+    }
+    auto pr2 = [&](const float(&a)[Q], int m) { return make_float2(a[2 * m], 2 * m + 1 < Q ? a[2 * m + 1] : 0.0f); };
+
+    // Per point pair: He column DIR, u.h and q.h, accumulators.
+    float2 h[H][3], cu[H], cq[H], acc[H][NACC];
+    int gidx[2 * H];
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+        float hv[2][3];
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            const int r = 2 * m + t;
+            if (r < Q) {
+                const int a = sPerm[line_lat<DIR, Q>(la, lb, r)];
+                gidx[r] = a;
+                const float *hp = He + ((size_t)(e < nelem ? e : 0) * N + a) * 9 + DIR * 3;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) hv[t][i] = ldg(hp + i);
+            } else {
+                gidx[r] = 0;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) hv[t][i] = 0.0f;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) h[m][i] = make_float2(hv[0][i], hv[1][i]);
+        const float2 u0 = pr2(u_[0], m), u1 = pr2(u_[1], m), u2 = pr2(u_[2], m);
+        const float2 q0 = pr2(q_[0], m), q1 = pr2(q_[1], m), q2 = pr2(q_[2], m);
+        cu[m] = fma2(u2, h[m][2], fma2(u1, h[m][1], mul2(u0, h[m][0])));
+        cq[m] = fma2(q2, h[m][2], fma2(q1, h[m][1], mul2(q0, h[m][0])));
+#pragma unroll
+        for (int k = 0; k < NACC; ++k) {
+            if (DIR == 0) {
+                acc[m][k] = f2(0.0f);
+            } else {
+                const int r1 = 2 * m + 1 < Q ? 2 * m + 1 : 2 * m;
+                acc[m][k] = make_float2(sA[k * NPL + base + 2 * m * OST], sA[k * NPL + base + r1 * OST]);
+            }
+        }
+    }
+
+    float2 d[H];
+    float f[Q];
+    auto deriv = [&](const float(&v)[Q]) {
+#pragma unroll
+        for (int m = 0; m < H; ++m) d[m] = f2(0.0f);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) {
+            const float2 vv = f2(v[c]);
+#pragma unroll
+            for (int m = 0; m < H; ++m) d[m] = fma2(c_CDp[P][(DIR * Q + c) * H + m], vv, d[m]);
+        }
+    };
+    const float2 h4 = f2(0.25f), h2 = f2(0.5f);
+
+    // rho: mass 1/2 u.grad rho, momentum 1/4 u_i u.grad rho, energy 1/4 H u.grad rho
+    deriv(rho_);
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+        const float2 t = mul2(cu[m], d[m]);
+        acc[m][A_M] = fma2(h2, t, acc[m][A_M]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) acc[m][A_MOM0 + i] = fma2(mul2(h4, pr2(u_[i], m)), t, acc[m][A_MOM0 + i]);
+        acc[m][A_E] = fma2(mul2(h4, pr2(H_, m)), t, acc[m][A_E]);
+    }
+    // p: grad p
+    deriv(p_);
+#pragma unroll
+    for (int m = 0; m < H; ++m)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) acc[m][A_MOM0 + i] = fma2(h[m][i], d[m], acc[m][A_MOM0 + i]);
+    // u_i: div u, 1/4 q.grad u_i ; q_i: div q, 1/4 u.grad q_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        deriv(u_[i]);
+#pragma unroll
+        for (int m = 0; m < H; ++m) {
+            acc[m][A_DIVU] = fma2(h[m][i], d[m], acc[m][A_DIVU]);
+            acc[m][A_MOM0 + i] = fma2(mul2(h4, cq[m]), d[m], acc[m][A_MOM0 + i]);
+        }
+        deriv(q_[i]);
+#pragma unroll
+        for (int m = 0; m < H; ++m) {
+            acc[m][A_DIVQ] = fma2(h[m][i], d[m], acc[m][A_DIVQ]);
+            acc[m][A_MOM0 + i] = fma2(mul2(h4, cu[m]), d[m], acc[m][A_MOM0 + i]);
+        }
+    }
+    // F_ij = q_i u_j: 1/4 div F_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+#pragma unroll
+            for (int c = 0; c < Q; ++c) f[c] = q_[i][c] * u_[j][c];
+            deriv(f);
+#pragma unroll
+            for (int m = 0; m < H; ++m) acc[m][A_MOM0 + i] = fma2(mul2(h4, h[m][j]), d[m], acc[m][A_MOM0 + i]);
+        }
+    // Fuu_ij = u_i u_j (symmetric): 1/4 rho div Fuu_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = i; j < 3; ++j) {
+#pragma unroll
+            for (int c = 0; c < Q; ++c) f[c] = u_[i][c] * u_[j][c];
+            deriv(f);
+#pragma unroll
+            for (int m = 0; m < H; ++m) {
+                const float2 rd = mul2(mul2(h4, pr2(rho_, m)), d[m]);
+                acc[m][A_MOM0 + i] = fma2(h[m][j], rd, acc[m][A_MOM0 + i]);
+                if (i != j) acc[m][A_MOM0 + j] = fma2(h[m][i], rd, acc[m][A_MOM0 + j]);
+            }
+        }
+    // H: 1/4 q.grad H ; rho H: 1/4 u.grad(rho H)
+    deriv(H_);
+#pragma unroll
+    for (int m = 0; m < H; ++m) acc[m][A_E] = fma2(mul2(h4, cq[m]), d[m], acc[m][A_E]);
+    deriv(rH_);
+#pragma unroll
+    for (int m = 0; m < H; ++m) acc[m][A_E] = fma2(mul2(h4, cu[m]), d[m], acc[m][A_E]);
+    // rho H u_i: 1/4 div(rho H u) ; H u_i: 1/4 rho div(H u)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = rH_[c] * u_[i][c];
+        deriv(f);
+#pragma unroll
+        for (int m = 0; m < H; ++m) acc[m][A_E] = fma2(mul2(h4, h[m][i]), d[m], acc[m][A_E]);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = H_[c] * u_[i][c];
+        deriv(f);
+#pragma unroll
+        for (int m = 0; m < H; ++m) acc[m][A_E] = fma2(mul2(mul2(h4, pr2(rho_, m)), h[m][i]), d[m], acc[m][A_E]);
+    }
+
+#pragma unroll
+    for (int r = 0; r < Q; ++r) {
+        const int m = r >> 1;
+        float a[NACC];
+#pragma unroll
+        for (int k = 0; k < NACC; ++k) a[k] = (r & 1) ? acc[m][k].y : acc[m][k].x;
+        const int o = base + r * OST;
+        if (DIR < 2) {
+#pragma unroll
+            for (int k = 0; k < NACC; ++k) sA[k * NPL + o] = a[k];
+        } else {
+            const int node = sNode[o];
+            if (node < 0 || e >= nelem) continue;
+            const float divU = a[A_DIVU], divQ = a[A_DIVQ];
+            const float gp = ldg(gpvol + (size_t)e * N + gidx[r]);
+            const float rm = a[A_M] + 0.5f * (divQ + rho_[r] * divU);
+            const float re = a[A_E] + 0.25f * (H_[r] * divQ + rH_[r] * divU);
+            red_add(Rmass + node, gp * rm);
+            red_add(Rener + node, gp * re);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float rmom = a[A_MOM0 + i] + 0.25f * (u_[i][r] * divQ + q_[i][r] * divU);
+                red_add(Rmom + (size_t)i * npoin + node, gp * rmom);
+            }
+        }
+    }
+}
+
+template <typename real, int P>
+constexpr bool convec_packed()
+{
+    return (CONVEC_X2 == 2 || (CONVEC_X2 == 1 && P == 5)) && sizeof(real) == 4 && ConvecGeom<real, P>::S == 1;
+}
+
+template <typename real, int P, int DIR>
+__device__ __forceinline__ void convec_dir(const real *sF, real *sA, const real *sD, const int *sNode,
+                                           const int *sPerm, const real *He, const real *gpvol, int e0, int nelem,
+                                           int npoin, real *Rmass, real *Rmom, real *Rener)
+{
+    if constexpr (convec_packed<real, P>())
+        convec_pass_x2<P, DIR>(sF, sA, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+    else
+        convec_pass<real, P, DIR>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+}
+
 // Blocks per SM the register budget is sized for: four 128-thread blocks (128
 // registers) when the derivative matrices are constant-bank operands.
 template <typename real, int P>
 constexpr int convec_minb()
 {
-    using G = LineGeom<real, P>;
-    return (sizeof(real) == 4 && G::S == 1 && G::NT <= 128 && P >= 3) ? CONVEC_MINB : 1;
+    using G = ConvecGeom<real, P>;
+    return (sizeof(real) == 4 && G::S == 1 && G::NT <= 128 && P >= 3) ? (P == 5 ? CONVEC_MINB5 : CONVEC_MINB)
+           : (sizeof(real) == 4 && G::S == 1 && P >= 3)               ? CONVEC_MINB_WIDE
+                                                                      : 1;
 }
 
 template <typename real, int P>
-__global__ void __launch_bounds__(LineGeom<real, P>::NT, convec_minb<real, P>())
+__global__ void __launch_bounds__(ConvecGeom<real, P>::NT, convec_minb<real, P>())
     convec_kernel(int nelem, int npoin, const int *__restrict__ connec, const real *__restrict__ He,
                   const real *__restrict__ gpvol, const real *__restrict__ dlxigp_ip,
                   const int *__restrict__ invAtoIJK, const int *__restrict__ AtoI,
@@ -292,7 +545,7 @@ __global__ void __launch_bounds__(LineGeom<real, P>::NT, convec_minb<real, P>())
                   real *__restrict__ Rmom,
                   real *__restrict__ Rener)
 {
-    using G = LineGeom<real, P>;
+    using G = ConvecGeom<real, P>;
     constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT;
     constexpr int NPL = NE * ES;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -353,17 +606,17 @@ __global__ void __launch_bounds__(LineGeom<real, P>::NT, convec_minb<real, P>())
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
-    convec_pass<real, P, 0>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+    convec_dir<real, P, 0>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
     __syncthreads();
-    convec_pass<real, P, 1>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+    convec_dir<real, P, 1>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
     __syncthreads();
-    convec_pass<real, P, 2>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+    convec_dir<real, P, 2>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
 }
 
 template <typename real, int P>
 constexpr size_t convec_smem()
 {
-    using G = LineGeom<real, P>;
+    using G = ConvecGeom<real, P>;
     return (size_t)(NFIELD + NACC) * G::NE * G::ES * sizeof(real) + 3 * G::Q * G::Q * sizeof(real) +
            (size_t)(G::NE * G::ES + 2 * G::N) * sizeof(int);
 }
@@ -371,7 +624,7 @@ constexpr size_t convec_smem()
 template <typename real, int P>
 cudaError_t launch_convec_p(const ConvecArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
-    using G = LineGeom<real, P>;
+    using G = ConvecGeom<real, P>;
     constexpr size_t smem = convec_smem<real, P>();
     static_assert(smem <= 227 * 1024, "shared memory budget");
     cudaError_t err = cudaFuncSetAttribute(convec_kernel<real, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -385,6 +638,12 @@ cudaError_t launch_convec_p(const ConvecArgs<real> &a, const TableScratch *tabs,
             err = cudaMemcpyToSymbolAsync(c_CDd, table_D<double>(tabs), sizeof(double) * 3 * G::Q * G::Q,
                                           sizeof(double) * kTableDMax * P, cudaMemcpyDeviceToDevice, st);
         if (err != cudaSuccess) return err;
+        if (convec_packed<real, P>()) {
+            constexpr int H = (G::Q + 1) / 2;
+            err = cudaMemcpyToSymbolAsync(c_CDp, tabs->Dp, sizeof(float2) * 3 * G::Q * H,
+                                          sizeof(float2) * (kTableDPairMax / 2) * P, cudaMemcpyDeviceToDevice, st);
+            if (err != cudaSuccess) return err;
+        }
     }
     const unsigned grid = (unsigned)((a.nelem + G::NE - 1) / G::NE);
     convec_kernel<real, P><<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.dlxigp_ip,

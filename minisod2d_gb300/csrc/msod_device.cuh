@@ -31,9 +31,10 @@ __device__ __forceinline__ T ldg(const T *p)
 //   Q  = points per line, L = lines per direction, N = points per element.
 //   QP = padded row pitch in shared memory (odd, so that line loads along x
 //        hit distinct banks), ES = shared-memory words per element plane.
-//   S  = threads per line (each owns R consecutive points of the line),
+//   S  = threads per line (each owns R consecutive points of the line; S_ > 0
+//        overrides the default),
 //   NE = elements per block (at most NECAP), NT = threads per block.
-template <typename real_t, int P_, int NECAP = 64>
+template <typename real_t, int P_, int NECAP = 64, int S_ = 0>
 struct LineGeom {
     using real = real_t;
     static constexpr int P = P_;
@@ -42,7 +43,7 @@ struct LineGeom {
     static constexpr int N = Q * Q * Q;
     static constexpr int QP = (Q % 2 == 0) ? Q + 1 : Q;
     static constexpr int ES = Q * Q * QP;
-    static constexpr int S = sizeof(real) == 8 ? Q : (P <= 5 ? 1 : (P <= 7 ? 2 : 3));
+    static constexpr int S = S_ > 0 ? S_ : (sizeof(real) == 8 ? Q : (P <= 5 ? 1 : (P <= 7 ? 2 : 3)));
     static constexpr int R = (Q + S - 1) / S;
     static constexpr int TPE = L * S;  // threads per element
     static constexpr int CAP = sizeof(real) == 8 ? (TPE <= 128 ? 128 : ((TPE + 31) / 32) * 32)

@@ -71,12 +71,20 @@ enum { P_NUE = 0, P_KAP = 1, P_DR = 2 };
 // thread's points, stored to planes sX[DIR*5 + f].
 template <class G, int DIR>
 __device__ __forceinline__ void grad_pass(const LineThread<G> &lt, const typename G::real *__restrict__ sF,
-                                          typename G::real *__restrict__ sX)
+                                          typename G::real *__restrict__ sX, const typename G::real *__restrict__ sD)
 {
     using real = typename G::real;
     constexpr int P = G::P, Q = G::Q, QP = G::QP, R = G::R, NPL = G::NPL;
     constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
     const int base = lt.el * G::ES + line_off<DIR, Q, QP>(lt.la, lt.lb, 0);
+    // Several threads per line: the thread's rows of the matrix, in registers
+    // for the pass (a per-lane index into the constant bank would serialise).
+    real Dr[G::S > 1 ? R : 1][Q];
+    if (G::S > 1)
+#pragma unroll
+        for (int rr = 0; rr < R; ++rr)
+#pragma unroll
+            for (int c = 0; c < Q; ++c) Dr[rr][c] = sD[(DIR * Q + lt.rc(rr)) * Q + c];
 #pragma unroll
     for (int f = 0; f < 5; ++f) {
         real v[Q];
@@ -85,10 +93,10 @@ __device__ __forceinline__ void grad_pass(const LineThread<G> &lt, const typenam
 #pragma unroll
         for (int rr = 0; rr < R; ++rr) {
             if (!lt.owns(rr)) continue;
-            const int row = G::S == 1 ? rr : lt.r0 + rr;
             real s = (real)0;
 #pragma unroll
-            for (int c = 0; c < Q; ++c) s = fma(cD<real>(P, (DIR * Q + row) * Q + c), v[c], s);
+            for (int c = 0; c < Q; ++c)
+                s = fma(G::S == 1 ? cD<real>(P, (DIR * Q + rr) * Q + c) : Dr[G::S == 1 ? 0 : rr][c], v[c], s);
             sX[(DIR * 5 + f) * NPL + base + (lt.r0 + rr) * OST] = s;
         }
     }
@@ -98,14 +106,21 @@ __device__ __forceinline__ void grad_pass(const LineThread<G> &lt, const typenam
 // derivative matrix; partial sums through planes P_DR.. of the stage.
 template <class G, int DIR>
 __device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::real *__restrict__ sF,
-                                         const typename G::real *__restrict__ sX, const int *__restrict__ sNode,
-                                         int npoin, typename G::real *__restrict__ Rmass,
-                                         typename G::real *__restrict__ Rmom, typename G::real *__restrict__ Rener)
+                                         const typename G::real *__restrict__ sX, const typename G::real *__restrict__ sD,
+                                         const int *__restrict__ sNode, int npoin,
+                                         typename G::real *__restrict__ Rmass, typename G::real *__restrict__ Rmom,
+                                         typename G::real *__restrict__ Rener)
 {
     using real = typename G::real;
     constexpr int P = G::P, Q = G::Q, QP = G::QP, R = G::R, NPL = G::NPL;
     constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
     const int base = lt.el * G::ES + line_off<DIR, Q, QP>(lt.la, lt.lb, 0);
+    real Dc[G::S > 1 ? R : 1][Q];  // several threads per line: the thread's columns
+    if (G::S > 1)
+#pragma unroll
+        for (int rr = 0; rr < R; ++rr)
+#pragma unroll
+            for (int c = 0; c < Q; ++c) Dc[rr][c] = sD[(DIR * Q + c) * Q + lt.rc(rr)];
     real acc[R][5], kap[R];
 #pragma unroll
     for (int rr = 0; rr < R; ++rr) {
@@ -121,10 +136,10 @@ __device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::re
         for (int c = 0; c < Q; ++c) v[c] = sX[(DIR * NX + x) * NPL + base + c * OST];
 #pragma unroll
         for (int rr = 0; rr < R; ++rr) {
-            const int col = G::S == 1 ? rr : lt.rc(rr);
             real s = (real)0;
 #pragma unroll
-            for (int c = 0; c < Q; ++c) s = fma(cD<real>(P, (DIR * Q + c) * Q + col), v[c], s);
+            for (int c = 0; c < Q; ++c)
+                s = fma(G::S == 1 ? cD<real>(P, (DIR * Q + c) * Q + rr) : Dc[G::S == 1 ? 0 : rr][c], v[c], s);
             if (x == X_GRHO) acc[rr][0] += s;
             else if (x == X_TAUU) acc[rr][1] += s;
             else if (x == X_GT) acc[rr][1] = fma(kap[rr], s, acc[rr][1]);
@@ -153,11 +168,29 @@ template <class G>
 constexpr size_t diffu_smem_bytes()
 {
     return (size_t)(DIFFU_NBUF * NDF + 3 * NX) * G::NPL * sizeof(typename G::real) +
+           (size_t)3 * G::Q * G::Q * sizeof(typename G::real) +
            (size_t)(DIFFU_NBUF * G::NPL + 2 * G::N) * sizeof(int);
 }
 
+// Threads per line of the FP32 diffusion (0: the line-geometry default, one).
+// Measured on 64^3 hexes: porder 4 is fastest with one (1.84 ms; 2.08-2.27 ms
+// with 2, 3 or 5: more warps, but the line loads are repeated per thread),
+// porder 5 with two (3.79 ms against 3.99 ms with one).
+#ifndef DIFFU_S4
+#define DIFFU_S4 0
+#endif
+#ifndef DIFFU_S5
+#define DIFFU_S5 2
+#endif
 template <typename real, int P>
-using DiffuGeom = LineGeom<real, P, necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES, (int)sizeof(real), 200 * 1024)>;
+constexpr int diffu_s()
+{
+    return sizeof(real) == 4 ? (P == 4 ? DIFFU_S4 : (P == 5 ? DIFFU_S5 : 0)) : 0;
+}
+
+template <typename real, int P>
+using DiffuGeom = LineGeom<real, P, necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES, (int)sizeof(real), 200 * 1024),
+                           diffu_s<real, P>()>;
 
 // Viscosity source of the diffusion kernel.
 enum { VISC_MU_E = 0, VISC_NU_ELEM = 1, VISC_NET = 2 };
@@ -193,7 +226,8 @@ __global__ void __launch_bounds__(G::NT)
     constexpr int NBUF = DIFFU_NBUF;
     real *sF = reinterpret_cast<real *>(smem_raw);  // [NBUF][NDF][NPL]
     real *sX = sF + NBUF * NDF * NPL;                // [3*NX][NPL]
-    int *sNode = reinterpret_cast<int *>(sX + 3 * NX * NPL);  // [NBUF][NPL]
+    real *sD = sX + 3 * NX * NPL;                    // [3][Q][Q] (several threads per line)
+    int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);  // [NBUF][NPL]
     int *sPerm = sNode + NBUF * NPL;
     int *sLat = sPerm + N;
     float *sNet = reinterpret_cast<float *>(sLat + N);  // network mode: weights, then per-group data
@@ -205,6 +239,8 @@ __global__ void __launch_bounds__(G::NT)
         sPerm[i] = tabs->perm[i];
         sLat[i] = tabs->lat[i];
     }
+    if (G::S > 1)
+        for (int i = tid; i < 3 * Q * Q; i += NT) sD[i] = table_D<real>(tabs)[i];
     if (VISC == VISC_NET) {
         for (int i = tid; i < kMlpParams; i += NT) {
             const float w = __half2float(net.wh[i]);
@@ -393,9 +429,9 @@ __global__ void __launch_bounds__(G::NT)
         }
         run_net(g);
         if (lt.active) {
-            grad_pass<G, 0>(lt, sFs, sX);
-            grad_pass<G, 1>(lt, sFs, sX);
-            grad_pass<G, 2>(lt, sFs, sX);
+            grad_pass<G, 0>(lt, sFs, sX, sD);
+            grad_pass<G, 1>(lt, sFs, sX, sD);
+            grad_pass<G, 2>(lt, sFs, sX, sD);
         }
         __syncthreads();
         // Point pass: physical gradients, stress and contravariant fluxes.
@@ -451,11 +487,11 @@ __global__ void __launch_bounds__(G::NT)
             sFs[P_KAP * NPL + o] = muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
         }
         __syncthreads();
-        if (lt.active) div_pass<G, 0>(lt, sFs, sX, sNs, npoin, Rmass, Rmom, Rener);
+        if (lt.active) div_pass<G, 0>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
         __syncthreads();
-        if (lt.active) div_pass<G, 1>(lt, sFs, sX, sNs, npoin, Rmass, Rmom, Rener);
+        if (lt.active) div_pass<G, 1>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
         __syncthreads();
-        if (lt.active) div_pass<G, 2>(lt, sFs, sX, sNs, npoin, Rmass, Rmom, Rener);
+        if (lt.active) div_pass<G, 2>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
         __syncthreads();
         if (NBUF == 1 && gn < ngroups) {  // the next group's node ids, then its fields
             store_ids(ids, sNode);

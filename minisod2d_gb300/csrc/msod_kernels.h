@@ -14,9 +14,13 @@ namespace msod {
 // offset (lat).
 constexpr int kTableDMax = 3 * (MSOD_MAX_PORDER + 1) * (MSOD_MAX_PORDER + 1);
 constexpr int kTableNMax = (MSOD_MAX_PORDER + 1) * (MSOD_MAX_PORDER + 1) * (MSOD_MAX_PORDER + 1);
+// Row pairs of the FP32 matrices for packed (f32x2) contractions:
+// Dp[((d*Q + c)*H + m)*2 + t] = D[d][2m+t][c] (zero for 2m+t = Q), H = (Q+1)/2.
+constexpr int kTableDPairMax = 3 * (MSOD_MAX_PORDER + 1) * (MSOD_MAX_PORDER + 2);
 struct TableScratch {
     float Df[kTableDMax];
     double Dd[kTableDMax];
+    alignas(8) float Dp[kTableDPairMax];
     int perm[kTableNMax];
     int lat[kTableNMax];
 };

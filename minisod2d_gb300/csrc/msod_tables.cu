@@ -44,6 +44,19 @@ __global__ void table_prep_kernel(const int *__restrict__ invAtoIJK, const int *
         const int l = d == 0 ? r : (d == 1 ? r * Q : r * Q * Q);
         D[i] = dlxigp_ip[(size_t)(c * 3 + d) * N + sperm[l]];
     }
+    if (sizeof(real) == 4) {
+        constexpr int H = (Q + 1) / 2;
+        for (int i = threadIdx.x; i < 3 * Q * H * 2; i += blockDim.x) {
+            const int t = i & 1, m = (i >> 1) % H, c = (i >> 1) / H % Q, d = (i >> 1) / (H * Q);
+            const int r = 2 * m + t;
+            float v = 0.0f;
+            if (r < Q) {
+                const int l = d == 0 ? r : (d == 1 ? r * Q : r * Q * Q);
+                v = (float)dlxigp_ip[(size_t)(c * 3 + d) * N + sperm[l]];
+            }
+            out->Dp[i] = v;
+        }
+    }
 }
 
 template <typename real, int P>
