@@ -95,45 +95,6 @@ __device__ __forceinline__ int line_lat(int la, int lb, int r)
     return DIR == 0 ? (lb * Q + la) * Q + r : (DIR == 1 ? (lb * Q + r) * Q + la : (r * Q + lb) * Q + la);
 }
 
-// Per-call element tables in shared memory, read from the caller's
-// reference-layout arrays:
-//   perm[l]   lattice point l = (K*Q+J)*Q+I (SOD 1-D indices, 0-based) -> gmsh
-//             local node a (invAtoIJK - 1)
-//   lat[a]    gmsh local node a -> padded lattice offset (K*Q+J)*QP+I
-//             (from gmshAtoI/J/K)
-//   D[d][r][c] = dlxigp_ip(g, d, c) for a point g whose 1-D index in
-//             direction d is r: the 1-D derivative matrix the reference
-//             replicates per point (elem_hex.f90:43-44).
-// Indices are clamped into range, so malformed tables give wrong numbers
-// (caught by msod_check_element_tables), never out-of-bounds accesses.
-template <typename real, int P>
-__device__ __forceinline__ void load_element_tables(const int *__restrict__ invAtoIJK,
-                                                    const int *__restrict__ AtoI,
-                                                    const int *__restrict__ AtoJ,
-                                                    const int *__restrict__ AtoK,
-                                                    const real *__restrict__ dlxigp_ip, int *perm,
-                                                    int *lat, real *D, int tid, int nthreads)
-{
-    using G = LineGeom<real, P>;
-    constexpr int Q = G::Q, N = G::N;
-    for (int i = tid; i < N; i += nthreads) {
-        int a = ldg(invAtoIJK + i) - 1;
-        perm[i] = min(max(a, 0), N - 1);
-        int I = min(max(ldg(AtoI + i) - 1, 0), Q - 1);
-        int J = min(max(ldg(AtoJ + i) - 1, 0), Q - 1);
-        int K = min(max(ldg(AtoK + i) - 1, 0), Q - 1);
-        lat[i] = (K * Q + J) * G::QP + I;
-    }
-    __syncthreads();
-    for (int i = tid; i < 3 * Q * Q; i += nthreads) {
-        const int d = i / (Q * Q), r = (i / Q) % Q, c = i % Q;
-        const int l = d == 0 ? r : (d == 1 ? r * Q : r * Q * Q);
-        const int g = perm[l];
-        D[i] = ldg(dlxigp_ip + (size_t)(c * 3 + d) * N + g);
-    }
-}
-
-
 // Order-preserving map of a float onto a signed int (for integer atomics).
 __device__ __forceinline__ int f2key(float f)
 {

@@ -149,6 +149,7 @@ struct ViscArgs {
     const EntropyStats *stats;
     const int *only;     // if set: process only elements with only[e] != 0, write nu only
     float *mu_e, *nu, *numax;
+    const TableScratch *tabs;  // the call's element tables (table_prep_kernel)
 };
 
 struct FeatureArgs {

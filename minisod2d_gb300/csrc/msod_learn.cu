@@ -83,6 +83,27 @@ int run_stats(int npoin, const float *rho, const float *p_or_T, float Rgas, floa
     return cuda_rc(launch_entropy_stats(npoin, rho, p_or_T, Rgas, gamma, s, st), "entropy statistics launch");
 }
 
+// The call's element tables (perm, lat, derivative matrices) in the
+// library-owned table area, prepared on the call's stream.
+int prep_tables(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
+                const float *dlxigp_ip, const int *invAtoIJK, const int *AtoI, const int *AtoJ, const int *AtoK,
+                TableScratch **out, cudaStream_t st)
+{
+    auto *tabs = static_cast<TableScratch *>(scratch(SLOT_TABLES, sizeof(TableScratch)));
+    if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
+    *out = tabs;
+    ElementArgs<float> ea{};
+    ea.nelem = nelem; ea.npoin = npoin; ea.connec = connec; ea.He = He; ea.gpvol = gpvol; ea.dlxigp_ip = dlxigp_ip;
+    ea.invAtoIJK = invAtoIJK; ea.AtoI = AtoI; ea.AtoJ = AtoJ; ea.AtoK = AtoK;
+    return cuda_rc(launch_table_prep<float>(porder, ea, tabs, st), "table preparation launch");
+}
+
+// The tables prepared by the last prep_tables call on this device.
+const TableScratch *prepared_tables()
+{
+    return static_cast<TableScratch *>(scratch(SLOT_TABLES, sizeof(TableScratch)));
+}
+
 uint32_t crc32(const unsigned char *p, size_t n)
 {
     uint32_t c = 0xFFFFFFFFu;
@@ -128,11 +149,16 @@ int msod_entropy_viscosity(int porder, int nelem, int npoin, const int *connec, 
     EntropyStats *stats = nullptr;
     rc = run_stats(npoin, rho, pr, 0.0f, gamma, &stats, st);
     if (rc) return rc;
+    TableScratch *tabs = nullptr;
+    rc = prep_tables(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                     &tabs, st);
+    if (rc) return rc;
     ViscArgs a{};
     a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlxigp_ip;
     a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
     a.rho = rho; a.u = u; a.p_or_T = pr; a.Rgas = 0.0f; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
     a.normalise = normalise; a.stats = stats; a.only = nullptr; a.mu_e = mu_e; a.nu = nu_elem; a.numax = numax_elem;
+    a.tabs = tabs;
     return cuda_rc(launch_entropy_visc(porder, a, st), "entropy viscosity launch");
 }
 
@@ -166,12 +192,9 @@ static int features_impl(int porder, int nelem, int npoin, const int *connec, co
     EntropyStats *stats = nullptr;
     rc = run_stats(npoin, rho, p_or_T, Rgas, gamma, &stats, st);
     if (rc) return rc;
-    auto *tabs = static_cast<TableScratch *>(scratch(SLOT_TABLES, sizeof(TableScratch)));
-    if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
-    ElementArgs<float> ea{};
-    ea.nelem = nelem; ea.npoin = npoin; ea.connec = connec; ea.He = He; ea.gpvol = gpvol; ea.dlxigp_ip = dlxigp_ip;
-    ea.invAtoIJK = invAtoIJK; ea.AtoI = gmshAtoI; ea.AtoJ = gmshAtoJ; ea.AtoK = gmshAtoK;
-    rc = cuda_rc(launch_table_prep<float>(porder, ea, tabs, st), "table preparation launch");
+    TableScratch *tabs = nullptr;
+    rc = prep_tables(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                     &tabs, st);
     if (rc) return rc;
     FeatureArgs fa{};
     fa.nelem = nelem; fa.npoin = npoin; fa.connec = connec; fa.He = He; fa.gpvol = gpvol; fa.tabs = tabs;
@@ -415,6 +438,7 @@ int msod_learned_viscosity(const msod_mlp *m, int porder, int nelem, int npoin, 
     a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
     a.rho = rho; a.u = u; a.p_or_T = p_or_T; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
     a.normalise = 1; a.stats = stats; a.only = fl; a.mu_e = nullptr; a.nu = nu_elem; a.numax = nullptr;
+    a.tabs = prepared_tables();  // prepared by the feature call above
     return cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
 }
 
@@ -449,6 +473,7 @@ int msod_diffusion_ijk_learned(const msod_mlp *m, int porder, int nelem, int npo
     a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
     a.rho = rho; a.u = u; a.p_or_T = p_or_T; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
     a.normalise = 1; a.stats = stats; a.only = fl; a.mu_e = nullptr; a.nu = nu_fb; a.numax = nullptr;
+    a.tabs = prepared_tables();  // prepared by the feature call above
     rc = cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
     if (rc) return rc;
     // 3. the diffusion, with the network evaluated in its prologue

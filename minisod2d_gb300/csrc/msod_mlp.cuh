@@ -12,6 +12,21 @@ __device__ __forceinline__ float sigmoidf_(float a) { return 1.0f / (1.0f + __ex
 __device__ __forceinline__ float softplus(float z) { return z > 20.0f ? z : log1pf(__expf(z)); }
 // Heavy-tailed non-negative features enter as logarithms (offset 1e-12).
 __device__ __forceinline__ float flog(float v) { return logf(fmaxf(v, 0.0f) + 1e-12f); }
+// Hardware approximations (PTX sqrt.approx.f32, lg2.approx.f32; div.full.f32
+// through __fdividef), about 1e-7 relative: the per-node statistics of the
+// features, far inside the features' own tolerance.
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+    float y;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float log2_approx(float x)
+{
+    float y;
+    asm("lg2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 // The network's output s >= 0 is a number of decades: y = 10^-s.  Targets y
 // are mapped to s = -log10(max(y, 1e-12)) for the loss.
 __device__ __forceinline__ float y_from_s(float s) { return exp10f(-s); }

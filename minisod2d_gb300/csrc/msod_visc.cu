@@ -92,6 +92,11 @@ __global__ void entropy_stats_kernel(int npoin, const float *__restrict__ rho, c
 // ---------------------------------------------------------------------------
 // Plain estimator: one group of NE elements per block, one thread per line.
 // ---------------------------------------------------------------------------
+// 1-D derivative matrices of the current call, per porder (copied from the
+// call's table area before the launch): constant-bank operands of the line
+// passes when one thread owns a line.
+__constant__ float c_VD[MSOD_MAX_PORDER + 1][kTableDMax];
+
 enum { V_RHO = 0, V_P, V_U0, V_U1, V_U2, NVF };
 constexpr int V_ETA = V_P;  // after the per-point preparation the pressure plane holds eta
 
@@ -127,7 +132,7 @@ __device__ __forceinline__ void residual_pass(const LineThread<G> &lt, const flo
         float dv[3] = {0.0f, 0.0f, 0.0f}, deu[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
         for (int c = 0; c < Q; ++c) {
-            const float d = sD[(DIR * Q + r) * Q + c];
+            const float d = G::S == 1 ? c_VD[G::P][(DIR * Q + rr) * Q + c] : sD[(DIR * Q + r) * Q + c];
             deta = fmaf(d, eta[c], deta);
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
@@ -157,12 +162,11 @@ __device__ __forceinline__ void residual_pass(const LineThread<G> &lt, const flo
 template <class G>
 __global__ void __launch_bounds__(G::NT)
     entropy_visc_kernel(int nelem, int npoin, const int *__restrict__ connec, const float *__restrict__ He,
-                        const float *__restrict__ gpvol, const float *__restrict__ dlxigp_ip,
-                        const int *__restrict__ invAtoIJK, const int *__restrict__ AtoI, const int *__restrict__ AtoJ,
-                        const int *__restrict__ AtoK, const float *__restrict__ rho, const float *__restrict__ u,
+                        const float *__restrict__ gpvol, const float *__restrict__ rho, const float *__restrict__ u,
                         const float *__restrict__ p_or_T, float Rgas, float gamma, float ce, float cmax,
                         int normalise, const EntropyStats *__restrict__ st, const int *__restrict__ only,
-                        float *__restrict__ mu_e, float *__restrict__ nu_out, float *__restrict__ numax_out)
+                        float *__restrict__ mu_e, float *__restrict__ nu_out, float *__restrict__ numax_out,
+                        const TableScratch *__restrict__ tabs)
 {
     constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT, NPL = G::NPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -172,8 +176,8 @@ __global__ void __launch_bounds__(G::NT)
     int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);
     int *sPerm = sNode + NPL;
     int *sLat = sPerm + N;
-    __shared__ int s_kR[NE], s_kS[NE];
-    __shared__ float s_vol[NE];
+    __shared__ int s_kS[NE];
+    __shared__ float s_vol[NE], s_nu[NE];
 
     const int tid = threadIdx.x;
     const int e0 = blockIdx.x * NE;
@@ -188,20 +192,34 @@ __global__ void __launch_bounds__(G::NT)
         __syncthreads();
         if (!s_any) return;
     }
-    load_element_tables<float, G::P>(invAtoIJK, AtoI, AtoJ, AtoK, dlxigp_ip, sPerm, sLat, sD, tid, NT);
+    // Node ids of the group (connec is element-fastest) into registers while
+    // the call's tables are copied into shared memory.
+    constexpr int IPT = (NE * N + NT - 1) / NT;
+    int ids[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = tid + k * NT;
+        const int el = i % NE, a = i / NE, e = e0 + el;
+        ids[k] = (i < NE * N && e < nelem) ? ldg(connec + (size_t)a * nelem + e) - 1 : -1;
+    }
+    for (int i = tid; i < N; i += NT) {
+        sPerm[i] = tabs->perm[i];
+        sLat[i] = tabs->lat[i];
+    }
+    if (G::S > 1)
+        for (int i = tid; i < 3 * Q * Q; i += NT) sD[i] = tabs->Df[i];
     if (tid < NE) {
-        s_kR[tid] = 0;
         s_kS[tid] = 0;
         s_vol[tid] = 0.0f;
     }
-    for (int i = tid; i < NE * N; i += NT) {
-        const int el = i % NE, a = i / NE, e = e0 + el;
-        int node = -1;
-        if (e < nelem) {
-            const int v = ldg(connec + (size_t)a * nelem + e) - 1;
-            node = (v >= 0 && v < npoin) ? v : -1;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = tid + k * NT;
+        if (i < NE * N) {
+            const int v = ids[k];
+            sNode[(i % NE) * ES + sLat[i / NE]] = (v >= 0 && v < npoin) ? v : -1;
         }
-        sNode[el * ES + sLat[a]] = node;
     }
     __syncthreads();
     const size_t np = (size_t)npoin;
@@ -259,21 +277,6 @@ __global__ void __launch_bounds__(G::NT)
     __syncthreads();
     if (live) residual_pass<G, 2>(lt, sF, sR, sPerm, sD, He, e, gamma);
     __syncthreads();
-    // Element maxima of |R| (one warp per element).
-    {
-        const int lane = tid & 31, warp = tid >> 5;
-        for (int el = warp; el < NE; el += NT / 32) {
-            unsigned mx = 0u;
-            if (e0 + el < nelem)
-                for (int l = lane; l < N; l += 32) {
-                    const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
-                    mx = max(mx, __float_as_uint(fabsf(sR[o])));
-                }
-            mx = __reduce_max_sync(0xffffffffu, mx);
-            if (lane == 0) s_kR[el] = (int)mx;
-        }
-    }
-    __syncthreads();
     float neta = 1.0f;
     if (normalise) {
         const double mean = st->sum / (double)npoin;
@@ -281,23 +284,41 @@ __global__ void __launch_bounds__(G::NT)
         neta = (float)fmax(hi - mean, mean - lo);
         if (!(neta > 0.0f)) neta = 1.0f;
     }
+    // Element maxima of |R| and the element viscosity (one warp per element).
+    {
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int el = warp; el < NE; el += NT / 32) {
+            const int ee = e0 + el;
+            unsigned mx = 0u;
+            if (ee < nelem)
+                for (int l = lane; l < N; l += 32) {
+                    const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
+                    mx = max(mx, __float_as_uint(fabsf(sR[o])));
+                }
+            mx = __reduce_max_sync(0xffffffffu, mx);
+            if (lane == 0) {
+                const float h = cbrtf(s_vol[el]) / (float)(Q - 1);
+                const float numax = cmax * h * __int_as_float(s_kS[el]);
+                const float nuE = ce * h * h * __uint_as_float(mx) / neta;
+                const float nu = fminf(numax, nuE);
+                s_nu[el] = nu;
+                if (ee < nelem) {
+                    if (only) {
+                        if (only[ee]) nu_out[ee] = nu;
+                    } else {
+                        if (nu_out) nu_out[ee] = nu;
+                        if (numax_out) numax_out[ee] = numax;
+                    }
+                }
+            }
+        }
+    }
+    if (only || !mu_e) return;
+    __syncthreads();
     for (int i = tid; i < NE * N; i += NT) {
         const int el = i % NE, a = i / NE, ee = e0 + el;
         if (ee >= nelem) continue;
-        const float h = cbrtf(s_vol[el]) / (float)(Q - 1);
-        const float numax = cmax * h * __int_as_float(s_kS[el]);
-        const float nuE = ce * h * h * __int_as_float(s_kR[el]) / neta;
-        const float nu = fminf(numax, nuE);
-        if (only) {
-            if (a == 0 && only[ee]) nu_out[ee] = nu;
-            continue;
-        }
-        const int o = el * ES + sLat[a];
-        if (mu_e) mu_e[(size_t)a * nelem + ee] = sF[V_RHO * NPL + o] * nu;
-        if (a == 0) {
-            if (nu_out) nu_out[ee] = nu;
-            if (numax_out) numax_out[ee] = numax;
-        }
+        mu_e[(size_t)a * nelem + ee] = sF[V_RHO * NPL + el * ES + sLat[a]] * s_nu[el];
     }
 }
 
@@ -312,12 +333,18 @@ cudaError_t visc_p(const ViscArgs &a, cudaStream_t st)
                             (size_t)(G::NPL + 2 * G::N) * sizeof(int);
     static_assert(smem <= 227 * 1024, "shared memory budget");
     auto kern = entropy_visc_kernel<G>;
+    if (!a.tabs) return cudaErrorInvalidValue;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
+    if (G::S == 1) {
+        err = cudaMemcpyToSymbolAsync(c_VD, a.tabs->Df, sizeof(float) * 3 * G::Q * G::Q, sizeof(float) * kTableDMax * P,
+                                      cudaMemcpyDeviceToDevice, st);
+        if (err != cudaSuccess) return err;
+    }
     const unsigned grid = (unsigned)((a.nelem + G::NE - 1) / G::NE);
-    kern<<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.dlxigp_ip, a.invAtoIJK, a.AtoI,
-                                    a.AtoJ, a.AtoK, a.rho, a.u, a.p_or_T, a.Rgas, a.gamma, a.ce, a.cmax, a.normalise,
-                                    a.stats, a.only, a.mu_e, a.nu, a.numax);
+    kern<<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.rho, a.u, a.p_or_T, a.Rgas, a.gamma,
+                                    a.ce, a.cmax, a.normalise,
+                                    a.stats, a.only, a.mu_e, a.nu, a.numax, a.tabs);
     return cudaGetLastError();
 }
 
