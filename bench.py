@@ -15,11 +15,12 @@ energy) for the full right-hand side.  Inputs (2.4 GB per call) exceed the
 Under torchrun each rank runs its own replica of the workload (weak scaling,
 no collective on the data path); rank 0 prints the max-over-ranks timing.
 
-On one GPU the line also carries "variants": the mixed-precision kernels on
-the 32^3 porder-7 workload, the learned viscosity on a held-out seed of the
-48^3 shock workload and the combined 96^3 porder-5 workload, each timed with
-CUDA events beside the plain kernels, with errors against the FP64 build of
-the plain kernels (--no-variants skips them).
+On one GPU the line also carries "variants": the linear-tetrahedron kernels
+on the reference driver's tet mesh over the plain_64 nodes, the
+mixed-precision kernels on the 32^3 porder-7 workload, the learned viscosity
+on a held-out seed of the 48^3 shock workload and the combined 96^3 porder-5
+workload, each timed with CUDA events, with errors against the FP64 build of
+the same kernels (--no-variants skips them).
 """
 import argparse
 import json
@@ -402,7 +403,7 @@ def run_ours(args, cfg, rank, local, world):
         out["cpu_baseline"] = cpu_baseline(cfg, host, args.cpu_seconds)
     if world == 1 and not args.no_variants:
         del dev
-        out["variants"] = run_variants()
+        out["variants"] = run_variants(host=host)
     print(json.dumps(out))
 
 
@@ -565,10 +566,41 @@ def variant_combined(reps):
             "nu_rel_l2_learned_vs_plain": _rel(nu_l, nu_p)}
 
 
-def run_variants(reps=10):
+def variant_tet(reps, host):
+    """tet_64: the driver's TET04 kernels (fem_convec, fem_diffu) on its
+    disconnected unit tetrahedra over the plain_64 node fields; errors against
+    the FP64 build of the same kernels on the same inputs."""
+    import torch
+
+    from minisod2d_gb300 import workload
+
+    tc = workload.TetCase(host)
+    peak, kind = peak_hbm()
+    res = {"workload": "tet_64: %d disconnected unit tetrahedra (the reference driver's TET04 mesh, "
+                       "mod_mesh.f90:71-126), %d nodes carrying the plain_64 fields, mu_e = mu_sgs = 1, "
+                       "Cp = Pr = 1" % (tc.nelem, tc.npoin),
+           "assembly": "red.global.add.v4.f32 (nodes 4k..4k+3)",
+           "error_reference": "FP64 build of the tet kernels on the same inputs"}
+    names = ("Rmass", "Rmom", "Rener")
+    t64 = workload.TetCase(host, dtype=torch.float64)
+    for which in ("convec", "diffu"):
+        fn32, fn64 = getattr(tc, which), getattr(t64, which)
+        ms = _ms(fn32, reps)
+        gbs = tc.algorithmic_bytes(which) / (ms * 1e-3) / 1e9
+        a, b = fn32(), fn64()
+        res[which] = {"ms": ms, "gbs": gbs, "frac": gbs / peak, "peak_gbs": peak, "peak_kind": kind,
+                      "algorithmic_bytes": tc.algorithmic_bytes(which),
+                      "err": {k: _rel(x, y) for k, x, y in zip(names, a, b)}}
+    del t64
+    return res
+
+
+def run_variants(reps=10, host=None):
     out = {}
-    for name, fn in (("mixed_p7", variant_mixed), ("learned_48", variant_learned),
-                     ("combined_96", variant_combined)):
+    variants = [("mixed_p7", variant_mixed), ("learned_48", variant_learned), ("combined_96", variant_combined)]
+    if host is not None:
+        variants.insert(0, ("tet_64", lambda r: variant_tet(r, host)))
+    for name, fn in variants:
         import torch
 
         try:

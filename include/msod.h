@@ -260,6 +260,63 @@ int msod_fields_recipe(int kind, int nmodes, uint64_t seed, int64_t npoin, const
                        float *mu_fluid);
 
 /* ---------------------------------------------------------------------------
+ * Linear tetrahedra (TET04): the reference driver's other timed kernels
+ * (main.f90:465-500).  4 nodes = 4 Gauss points per element; device arrays
+ * (E = nelem):
+ *     connec(nelem,4)     connec[a*E+e]           int32, 1-based
+ *     Ngp(4,4)            Ngp[c*4+r] = Ngp(r,c)   (the driver's Ngp(igaus,inode))
+ *     dNgp(3,4,4)         dNgp[(g*4+a)*3+d]
+ *     He(3,3,4,nelem)     He[((e*4+g)*3+j)*3+i]
+ *     gpvol(1,4,nelem)    gpvol[e*4+g]
+ *     mu_e,mu_sgs(nelem,4) mu_e[a*E+e]
+ * Outputs are intent(out).  Elements whose nodes are 4k..4k+3 (the driver's
+ * tet mesh) are assembled with 16-byte vector reductions when the residual
+ * arrays are 16-byte aligned and npoin is a multiple of 4.
+ * ------------------------------------------------------------------------- */
+
+/* fem_convec (elem_convec.f90:839-948): split-form convection on TET04
+ * elements, Ngp read as Ngp(igaus,inode). */
+int msod_fem_convec(int nelem, int npoin, const int *connec, const float *Ngp, const float *dNgp,
+                    const float *He, const float *gpvol, const float *u, const float *q, const float *rho,
+                    const float *pr, const float *E, float *Rmass, float *Rmom, float *Rener, void *stream);
+int msod_fem_convec_f64(int nelem, int npoin, const int *connec, const double *Ngp, const double *dNgp,
+                        const double *He, const double *gpvol, const double *u, const double *q,
+                        const double *rho, const double *pr, const double *E, double *Rmass, double *Rmom,
+                        double *Rener, void *stream);
+
+/* fem_diffu (elem_diffu.f90:199-317): viscous, heat and artificial mass
+ * diffusion on TET04 elements.  As in the reference it reads Ngp(inode,igaus)
+ * (the transpose of fem_convec's reading), interpolates mu and kappa to the
+ * Gauss points with kappa = mu_fluid Cp/Pr + mu_e/0.4 + rho mu_sgs/0.9, and
+ * applies mu to the whole stress including its -2/3 div u part. */
+int msod_fem_diffu(int nelem, int npoin, const int *connec, const float *Ngp, const float *dNgp,
+                   const float *He, const float *gpvol, float Cp, float Pr, const float *rho, const float *u,
+                   const float *Tem, const float *mu_fluid, const float *mu_e, const float *mu_sgs,
+                   float *Rmass, float *Rmom, float *Rener, void *stream);
+int msod_fem_diffu_f64(int nelem, int npoin, const int *connec, const double *Ngp, const double *dNgp,
+                       const double *He, const double *gpvol, double Cp, double Pr, const double *rho,
+                       const double *u, const double *Tem, const double *mu_fluid, const double *mu_e,
+                       const double *mu_sgs, double *Rmass, double *Rmom, double *Rener, void *stream);
+
+/* tet_jacobian (jacobian_oper.f90:138-267) on the device, rounded like
+ * msod_elem_jacobian. */
+int msod_tet_jacobian(int nelem, int npoin, const int *connec, const float *coord, const float *dNgp,
+                      const float *wgp, float *gpvol, float *He, void *stream);
+int msod_tet_jacobian_f64(int nelem, int npoin, const int *connec, const double *coord,
+                          const double *dNgp, const double *wgp, double *gpvol, double *He, void *stream);
+
+/* Host: tet_4points + tet_04 tables as the driver fills them (main.f90:377-383):
+ * Ngp[16], dNgp[48], xgp[12] (xgp[d*4+g]), wgp[4]. */
+int msod_tet_element_tables(float *Ngp, float *dNgp, float *xgp, float *wgp);
+int msod_tet_element_tables_f64(double *Ngp, double *dNgp, double *xgp, double *wgp);
+
+/* Host: the driver's disconnected tet mesh (gen_tet_mesh, mod_mesh.f90:71-126):
+ * npoin = 4 nelem, connec(e,a) = 4(e-1)+a, element e = xyzBase(4,3)
+ * (xyzBase[d*4+a]) shifted by 3(e-1) along every axis.  coord(npoin,3) may be
+ * NULL. */
+int msod_tet_mesh_disconnected(int nelem, const float *xyzBase, int *connec, float *coord);
+
+/* ---------------------------------------------------------------------------
  * Artificial viscosity mu_e: plain entropy-viscosity estimator and the
  * learned per-element estimator.  No counterpart in the reference, which
  * consumes mu_e(nelem,ngaus) (elem_diffu.f90:19) without computing it; the

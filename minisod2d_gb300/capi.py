@@ -57,6 +57,15 @@ SIGNATURES = {
     "msod_diffusion_ijk_f64": _GEOM64 + [_d, _d] + [_p] * 9 + [_p],
     "msod_check_element_tables": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
     "msod_check_element_tables_noalloc": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
+    "msod_fem_convec": [_i, _i] + [_p] * 13 + [_p],
+    "msod_fem_convec_f64": [_i, _i] + [_p] * 13 + [_p],
+    "msod_fem_diffu": [_i, _i] + [_p] * 5 + [_f, _f] + [_p] * 9 + [_p],
+    "msod_fem_diffu_f64": [_i, _i] + [_p] * 5 + [_d, _d] + [_p] * 9 + [_p],
+    "msod_tet_jacobian": [_i, _i] + [_p] * 6 + [_p],
+    "msod_tet_jacobian_f64": [_i, _i] + [_p] * 6 + [_p],
+    "msod_tet_element_tables": [_p] * 4,
+    "msod_tet_element_tables_f64": [_p] * 4,
+    "msod_tet_mesh_disconnected": [_i, _p, _p, _p],
     "msod_elem_jacobian": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
     "msod_elem_jacobian_f64": [_i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
     "msod_fem_element_tables": [_i] + [_p] * 10,

@@ -499,4 +499,131 @@ int msod_elem_jacobian_f64(int porder, int nelem, int npoin, const int *connec, 
                        "elem_jacobian launch");
 }
 
+// ---------------------------------------------------------------------------
+// Linear tetrahedra: fem_convec (elem_convec.f90:839), fem_diffu (elem_diffu.f90:199)
+// ---------------------------------------------------------------------------
+
+extern "C++" {
+static int tet_ok(int nelem, int npoin, const void *connec, const void *Ngp, const void *dNgp, const void *He,
+                  const void *gpvol)
+{
+    if (nelem < 1 || npoin < 1) return set_error(MSOD_ERR_INVALID_ARG, "nelem and npoin must be positive");
+    if ((long long)nelem * 4 >= (1LL << 31)) return set_error(MSOD_ERR_INVALID_ARG, "nelem*4 exceeds int32");
+    if (!connec || !Ngp || !dNgp || !He || !gpvol) return set_error(MSOD_ERR_INVALID_ARG, "NULL element array");
+    return MSOD_OK;
+}
+
+static int tet_check(int nelem, int npoin, const int *connec, cudaStream_t st)
+{
+    int *flags = device_flags();
+    if (!flags) return set_error(MSOD_ERR_CUDA, "could not allocate the validation flag");
+    int rc = cuda_status(cudaMemsetAsync(flags, 0, sizeof(int), st), "cudaMemsetAsync");
+    if (!rc) rc = cuda_status(launch_check_connec(4LL * nelem, npoin, connec, flags, st), "connec check launch");
+    int h = 0;
+    if (!rc) rc = cuda_status(cudaMemcpyAsync(&h, flags, sizeof(int), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+    if (!rc) rc = cuda_status(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (!rc && h) return set_error(MSOD_ERR_BAD_TABLES, "connec has entries outside 1..npoin");
+    return rc;
+}
+
+template <typename real>
+static int fem_convec_impl(int nelem, int npoin, const int *connec, const real *Ngp, const real *dNgp,
+                           const real *He, const real *gpvol, const real *u, const real *q, const real *rho,
+                           const real *pr, const real *E, real *Rmass, real *Rmom, real *Rener, void *stream)
+{
+    clear_error();
+    int rc = tet_ok(nelem, npoin, connec, Ngp, dNgp, He, gpvol);
+    if (rc) return rc;
+    if (!u || !q || !rho || !pr || !E || !Rmass || !Rmom || !Rener)
+        return set_error(MSOD_ERR_INVALID_ARG, "NULL field or residual array");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (checked_mode() && (rc = tet_check(nelem, npoin, connec, st))) return rc;
+    rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
+    if (rc) return rc;
+    TetConvecArgs<real> a{nelem, npoin, connec, Ngp, dNgp, He, gpvol, u, q, rho, pr, E, Rmass, Rmom, Rener};
+    return cuda_status(launch_fem_convec<real>(a, st), "fem_convec launch");
+}
+
+template <typename real>
+static int fem_diffu_impl(int nelem, int npoin, const int *connec, const real *Ngp, const real *dNgp,
+                          const real *He, const real *gpvol, real Cp, real Pr, const real *rho, const real *u,
+                          const real *Tem, const real *mu_fluid, const real *mu_e, const real *mu_sgs, real *Rmass,
+                          real *Rmom, real *Rener, void *stream)
+{
+    clear_error();
+    int rc = tet_ok(nelem, npoin, connec, Ngp, dNgp, He, gpvol);
+    if (rc) return rc;
+    if (!rho || !u || !Tem || !mu_fluid || !mu_e || !mu_sgs || !Rmass || !Rmom || !Rener)
+        return set_error(MSOD_ERR_INVALID_ARG, "NULL field or residual array");
+    if (Pr == (real)0) return set_error(MSOD_ERR_INVALID_ARG, "Pr must be nonzero");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (checked_mode() && (rc = tet_check(nelem, npoin, connec, st))) return rc;
+    rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
+    if (rc) return rc;
+    TetDiffuArgs<real> a{nelem, npoin, connec, Ngp, dNgp, He, gpvol, Cp, Pr,
+                         rho, u, Tem, mu_fluid, mu_e, mu_sgs, Rmass, Rmom, Rener};
+    return cuda_status(launch_fem_diffu<real>(a, st), "fem_diffu launch");
+}
+
+template <typename real>
+static int tet_jacobian_impl(int nelem, int npoin, const int *connec, const real *coord, const real *dNgp,
+                             const real *wgp, real *gpvol, real *He, void *stream)
+{
+    clear_error();
+    if (nelem < 1 || npoin < 1 || !connec || !coord || !dNgp || !wgp || !gpvol || !He)
+        return set_error(MSOD_ERR_INVALID_ARG, "bad sizes or NULL array");
+    return cuda_status(launch_jacobian_nodes<real>(4, nelem, npoin, connec, coord, dNgp, wgp, gpvol, He,
+                                                   static_cast<cudaStream_t>(stream)),
+                       "tet_jacobian launch");
+}
+
+}  // extern "C++"
+
+int msod_fem_convec(int nelem, int npoin, const int *connec, const float *Ngp, const float *dNgp, const float *He,
+                    const float *gpvol, const float *u, const float *q, const float *rho, const float *pr,
+                    const float *E, float *Rmass, float *Rmom, float *Rener, void *stream)
+{
+    return fem_convec_impl<float>(nelem, npoin, connec, Ngp, dNgp, He, gpvol, u, q, rho, pr, E, Rmass, Rmom, Rener,
+                                  stream);
+}
+
+int msod_fem_convec_f64(int nelem, int npoin, const int *connec, const double *Ngp, const double *dNgp,
+                        const double *He, const double *gpvol, const double *u, const double *q, const double *rho,
+                        const double *pr, const double *E, double *Rmass, double *Rmom, double *Rener,
+                        void *stream)
+{
+    return fem_convec_impl<double>(nelem, npoin, connec, Ngp, dNgp, He, gpvol, u, q, rho, pr, E, Rmass, Rmom,
+                                   Rener, stream);
+}
+
+int msod_fem_diffu(int nelem, int npoin, const int *connec, const float *Ngp, const float *dNgp, const float *He,
+                   const float *gpvol, float Cp, float Pr, const float *rho, const float *u, const float *Tem,
+                   const float *mu_fluid, const float *mu_e, const float *mu_sgs, float *Rmass, float *Rmom,
+                   float *Rener, void *stream)
+{
+    return fem_diffu_impl<float>(nelem, npoin, connec, Ngp, dNgp, He, gpvol, Cp, Pr, rho, u, Tem, mu_fluid, mu_e,
+                                 mu_sgs, Rmass, Rmom, Rener, stream);
+}
+
+int msod_fem_diffu_f64(int nelem, int npoin, const int *connec, const double *Ngp, const double *dNgp,
+                       const double *He, const double *gpvol, double Cp, double Pr, const double *rho,
+                       const double *u, const double *Tem, const double *mu_fluid, const double *mu_e,
+                       const double *mu_sgs, double *Rmass, double *Rmom, double *Rener, void *stream)
+{
+    return fem_diffu_impl<double>(nelem, npoin, connec, Ngp, dNgp, He, gpvol, Cp, Pr, rho, u, Tem, mu_fluid, mu_e,
+                                  mu_sgs, Rmass, Rmom, Rener, stream);
+}
+
+int msod_tet_jacobian(int nelem, int npoin, const int *connec, const float *coord, const float *dNgp,
+                      const float *wgp, float *gpvol, float *He, void *stream)
+{
+    return tet_jacobian_impl<float>(nelem, npoin, connec, coord, dNgp, wgp, gpvol, He, stream);
+}
+
+int msod_tet_jacobian_f64(int nelem, int npoin, const int *connec, const double *coord, const double *dNgp,
+                          const double *wgp, double *gpvol, double *He, void *stream)
+{
+    return tet_jacobian_impl<double>(nelem, npoin, connec, coord, dNgp, wgp, gpvol, He, stream);
+}
+
 }  // extern "C"

@@ -282,7 +282,49 @@ std::vector<Mode> make_modes(Rng &rng, int nmodes, int kmax, double amp_sigma)
     return m;
 }
 
+// tet_4points (quadrature_rules.f90:84-99) and tet_04 (elem_tet.f90:9-36) at
+// each point, filled as the driver fills its tet tables (main.f90:377-383):
+// Ngp(igaus,inode) = N_inode(x_igaus) at Ngp[inode*4+igaus], dNgp(:,inode,igaus)
+// at dNgp[(igaus*4+inode)*3+d], xgp(igaus,d) at xgp[d*4+igaus].  The two point
+// coordinates round to the same FP32 value from the decimal literal directly
+// or through FP64.
+template <typename real>
+void tet_tables(real *Ngp, real *dNgp, real *xgp, real *wgp)
+{
+    const real a = (real)0.5854101966249680, b = (real)0.1381966011250110;
+    const real X[4][3] = {{a, b, b}, {b, a, b}, {b, b, a}, {b, b, b}};
+    static const int dN[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int g = 0; g < 4; ++g) {
+        for (int d = 0; d < 3; ++d) xgp[d * 4 + g] = X[g][d];
+        wgp[g] = (real)0.25;
+        const real xi = X[g][0], eta = X[g][1], zeta = X[g][2];
+        const real N[4] = {(real)1 - xi - eta - zeta, xi, eta, zeta};
+        for (int k = 0; k < 4; ++k) {
+            Ngp[k * 4 + g] = N[k];
+            for (int d = 0; d < 3; ++d) dNgp[(g * 4 + k) * 3 + d] = (real)dN[k][d];
+        }
+    }
+}
+
+// gen_tet_mesh (mod_mesh.f90:71-126): connec(e,a) = (e-1)*4 + a, element e a
+// copy of xyzBase (xyzBase[d*4+a]) shifted by 3.0 per element along every axis.
+template <typename real>
+void tet_mesh(int nelem, const real *xyzBase, int *connec, real *coord)
+{
+    const int64_t npoin = 4 * (int64_t)nelem;
+    for (int64_t e = 0; e < nelem; ++e)
+        for (int a = 0; a < 4; ++a) connec[(int64_t)a * nelem + e] = (int)(e * 4 + a + 1);
+    if (!coord) return;
+    real xyz0 = (real)0;
+    for (int64_t e = 0; e < nelem; ++e) {
+        for (int a = 0; a < 4; ++a)
+            for (int d = 0; d < 3; ++d) coord[(int64_t)d * npoin + e * 4 + a] = xyzBase[d * 4 + a] + xyz0;
+        xyz0 = xyz0 + (real)3;
+    }
+}
+
 }  // namespace
+
 
 extern "C" {
 
@@ -422,6 +464,30 @@ int msod_fields_recipe(int kind, int nmodes, uint64_t seed, int64_t npoin, const
         Tem[p] = pf / (rf * (float)Rgas);
         mu_fluid[p] = 1.8e-5f;
     }
+    return MSOD_OK;
+}
+
+
+int msod_tet_element_tables(float *Ngp, float *dNgp, float *xgp, float *wgp)
+{
+    if (!Ngp || !dNgp || !xgp || !wgp) return msod::set_error(MSOD_ERR_INVALID_ARG, "NULL table");
+    tet_tables<float>(Ngp, dNgp, xgp, wgp);
+    return MSOD_OK;
+}
+
+int msod_tet_element_tables_f64(double *Ngp, double *dNgp, double *xgp, double *wgp)
+{
+    if (!Ngp || !dNgp || !xgp || !wgp) return msod::set_error(MSOD_ERR_INVALID_ARG, "NULL table");
+    tet_tables<double>(Ngp, dNgp, xgp, wgp);
+    return MSOD_OK;
+}
+
+int msod_tet_mesh_disconnected(int nelem, const float *xyzBase, int *connec, float *coord)
+{
+    if (nelem < 1 || (int64_t)nelem * 4 >= ((int64_t)1 << 31))
+        return msod::set_error(MSOD_ERR_INVALID_ARG, "nelem must be in 1..2^29-1");
+    if (!connec || (coord && !xyzBase)) return msod::set_error(MSOD_ERR_INVALID_ARG, "NULL array");
+    tet_mesh<float>(nelem, xyzBase, connec, coord);
     return MSOD_OK;
 }
 

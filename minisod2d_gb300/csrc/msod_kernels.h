@@ -138,6 +138,36 @@ struct MlpNorm {
     float mean[kMlpIn], inv_std[kMlpIn], fmin[kMlpIn], fmax[kMlpIn];
 };
 
+// Linear tetrahedra (fem_convec, fem_diffu): 4 nodes, 4 Gauss points; tables
+// Ngp(4,4), dNgp(3,4,4) are device arrays in the reference's layouts.
+template <typename real>
+struct TetConvecArgs {
+    int nelem, npoin;
+    const int *connec;
+    const real *Ngp, *dNgp, *He, *gpvol;
+    const real *u, *q, *rho, *pr, *E;
+    real *Rmass, *Rmom, *Rener;
+};
+template <typename real>
+struct TetDiffuArgs {
+    int nelem, npoin;
+    const int *connec;
+    const real *Ngp, *dNgp, *He, *gpvol;
+    real Cp, Pr;
+    const real *rho, *u, *Tem, *mu_fluid, *mu_e, *mu_sgs;
+    real *Rmass, *Rmom, *Rener;
+};
+template <typename real>
+cudaError_t launch_fem_convec(const TetConvecArgs<real> &a, cudaStream_t st);
+template <typename real>
+cudaError_t launch_fem_diffu(const TetDiffuArgs<real> &a, cudaStream_t st);
+// Range check of count connec entries against 1..npoin (sets bit 8 of flags).
+cudaError_t launch_check_connec(long long count, int npoin, const int *connec, int *flags, cudaStream_t st);
+// Jacobian of elements with n nodes = n points (elem_jacobian / tet_jacobian).
+template <typename real>
+cudaError_t launch_jacobian_nodes(int n, int nelem, int npoin, const int *connec, const real *coord,
+                                  const real *dNgp, const real *wgp, real *gpvol, real *He, cudaStream_t st);
+
 struct ViscArgs {
     int nelem, npoin;
     const int *connec;

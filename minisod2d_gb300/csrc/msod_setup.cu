@@ -125,15 +125,27 @@ __global__ void check_tables_kernel(int P, int nelem, int npoin, const int *__re
 }  // namespace
 
 template <typename real>
-cudaError_t launch_elem_jacobian(int porder, int nelem, int npoin, const int *connec, const real *coord,
-                                 const real *dNgp, const real *wgp, real *gpvol, real *He, cudaStream_t st)
+cudaError_t launch_jacobian_nodes(int n, int nelem, int npoin, const int *connec, const real *coord,
+                                  const real *dNgp, const real *wgp, real *gpvol, real *He, cudaStream_t st)
 {
-    const int n = (porder + 1) * (porder + 1) * (porder + 1);
-    const int threads = n <= 128 ? 128 : (n <= 256 ? 256 : (n <= 512 ? 512 : 768));
+    const int threads = n <= 32 ? 32 : (n <= 128 ? 128 : (n <= 256 ? 256 : (n <= 512 ? 512 : 768)));
     const size_t smem = 3 * (size_t)n * sizeof(real);
     elem_jacobian_kernel<real><<<nelem, threads, smem, st>>>(n, nelem, npoin, connec, coord, dNgp, wgp, gpvol, He);
     return cudaGetLastError();
 }
+
+template <typename real>
+cudaError_t launch_elem_jacobian(int porder, int nelem, int npoin, const int *connec, const real *coord,
+                                 const real *dNgp, const real *wgp, real *gpvol, real *He, cudaStream_t st)
+{
+    const int n = (porder + 1) * (porder + 1) * (porder + 1);
+    return launch_jacobian_nodes<real>(n, nelem, npoin, connec, coord, dNgp, wgp, gpvol, He, st);
+}
+
+template cudaError_t launch_jacobian_nodes<float>(int, int, int, const int *, const float *, const float *,
+                                                  const float *, float *, float *, cudaStream_t);
+template cudaError_t launch_jacobian_nodes<double>(int, int, int, const int *, const double *, const double *,
+                                                   const double *, double *, double *, cudaStream_t);
 
 template cudaError_t launch_elem_jacobian<float>(int, int, int, const int *, const float *, const float *,
                                                  const float *, float *, float *, cudaStream_t);

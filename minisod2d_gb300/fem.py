@@ -66,3 +66,29 @@ def fields_recipe(kind, nmodes, seed, npoin, coord):
     capi.call("msod_fields_recipe", int(kind), int(nmodes), int(seed) & (2 ** 64 - 1), int(npoin), _p(coord),
               _p(f["rho"]), _p(f["u"]), _p(f["q"]), _p(f["pr"]), _p(f["E"]), _p(f["Tem"]), _p(f["mu_fluid"]))
     return f
+
+
+# ---------------------------------------------------------------------------
+# Linear tetrahedra (the reference driver's TET04 data, main.f90:365-407)
+# ---------------------------------------------------------------------------
+
+def tet_element_tables(dtype=np.float32):
+    """tet_4points + tet_04 tables: Ngp[a*4+g] (Ngp(igaus,inode)), dNgp[(g*4+a)*3+d],
+    xgp[d*4+g], wgp[4]."""
+    t = dict(Ngp=np.zeros(16, dtype), dNgp=np.zeros(48, dtype), xgp=np.zeros(12, dtype), wgp=np.zeros(4, dtype))
+    name = "msod_tet_element_tables" if np.dtype(dtype) == np.float32 else "msod_tet_element_tables_f64"
+    capi.call(name, _p(t["Ngp"]), _p(t["dNgp"]), _p(t["xgp"]), _p(t["wgp"]))
+    return t
+
+
+# xyzTET of the driver (main.f90:390-393) as xyzBase[d*4+a].
+TET_BASE = np.array([0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1], np.float32)
+
+
+def tet_mesh_disconnected(nelem, xyzBase=TET_BASE, coords=True):
+    """The driver's disconnected tet mesh (gen_tet_mesh): (connec[a*nelem+e], coord or None, npoin = 4 nelem)."""
+    connec = np.zeros(4 * nelem, np.int32)
+    coord = np.zeros(3 * 4 * nelem, np.float32) if coords else None
+    base = np.ascontiguousarray(xyzBase, np.float32)
+    capi.call("msod_tet_mesh_disconnected", int(nelem), _p(base), _p(connec), _p(coord) if coords else None)
+    return connec, coord, 4 * nelem

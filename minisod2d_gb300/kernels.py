@@ -163,6 +163,57 @@ def elem_jacobian(porder, nelem, npoin, connec, coord, dNgp, wgp, gpvol, He, str
     capi.call(name, int(porder), nelem, npoin, *args, _stream(stream))
 
 
+def _tet_geometry(nelem, connec, Ngp, dNgp, He, gpvol, real):
+    import torch
+
+    return [_ptr(connec, "connec", torch.int32, 4 * nelem), _ptr(Ngp, "Ngp", real, 16),
+            _ptr(dNgp, "dNgp", real, 48), _ptr(He, "He", real, 36 * nelem), _ptr(gpvol, "gpvol", real, 4 * nelem)]
+
+
+def fem_convec(nelem, npoin, connec, Ngp, dNgp, He, gpvol, u, q, rho, pr, E, Rmass, Rmom, Rener, stream=None):
+    """elem_convec.f90:839 (linear tetrahedra)."""
+    import torch
+
+    real = He.dtype
+    g = _tet_geometry(nelem, connec, Ngp, dNgp, He, gpvol, real)
+    f = [_ptr(u, "u", real, 3 * npoin), _ptr(q, "q", real, 3 * npoin), _ptr(rho, "rho", real, npoin),
+         _ptr(pr, "pr", real, npoin), _ptr(E, "E", real, npoin), _ptr(Rmass, "Rmass", real, npoin),
+         _ptr(Rmom, "Rmom", real, 3 * npoin), _ptr(Rener, "Rener", real, npoin)]
+    if real not in (torch.float32, torch.float64):
+        raise TypeError("He must be float32 or float64")
+    name = "msod_fem_convec" if real == torch.float32 else "msod_fem_convec_f64"
+    capi.call(name, nelem, npoin, *g, *f, _stream(stream))
+
+
+def fem_diffu(nelem, npoin, connec, Ngp, dNgp, He, gpvol, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs, Rmass, Rmom,
+              Rener, stream=None):
+    """elem_diffu.f90:199 (linear tetrahedra)."""
+    import torch
+
+    real = He.dtype
+    g = _tet_geometry(nelem, connec, Ngp, dNgp, He, gpvol, real)
+    f = [_ptr(rho, "rho", real, npoin), _ptr(u, "u", real, 3 * npoin), _ptr(Tem, "Tem", real, npoin),
+         _ptr(mu_fluid, "mu_fluid", real, npoin), _ptr(mu_e, "mu_e", real, 4 * nelem),
+         _ptr(mu_sgs, "mu_sgs", real, 4 * nelem), _ptr(Rmass, "Rmass", real, npoin),
+         _ptr(Rmom, "Rmom", real, 3 * npoin), _ptr(Rener, "Rener", real, npoin)]
+    if real not in (torch.float32, torch.float64):
+        raise TypeError("He must be float32 or float64")
+    name = "msod_fem_diffu" if real == torch.float32 else "msod_fem_diffu_f64"
+    capi.call(name, nelem, npoin, *g, float(Cp), float(Pr), *f, _stream(stream))
+
+
+def tet_jacobian(nelem, npoin, connec, coord, dNgp, wgp, gpvol, He, stream=None):
+    """jacobian_oper.f90:138 on the device; writes gpvol and He in place."""
+    import torch
+
+    real = coord.dtype
+    args = [_ptr(connec, "connec", torch.int32, 4 * nelem), _ptr(coord, "coord", real, 3 * npoin),
+            _ptr(dNgp, "dNgp", real, 48), _ptr(wgp, "wgp", real, 4), _ptr(gpvol, "gpvol", real, 4 * nelem),
+            _ptr(He, "He", real, 36 * nelem)]
+    name = "msod_tet_jacobian" if real == torch.float32 else "msod_tet_jacobian_f64"
+    capi.call(name, nelem, npoin, *args, _stream(stream))
+
+
 def check_element_tables(porder, nelem, npoin, connec, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
                          stream=None):
     import torch

@@ -9,7 +9,9 @@ Builds a structured mesh (``--nx``^3 hexes, ``--jitter``) with seeded fields
 convec_mixed, diffu_mixed (``--precision`` fp16 / bf16), estimator (plain
 entropy viscosity), learned (features + network + fallback, with a freshly
 initialised network unless ``--weights`` names a weight file), diffu_learned
-(the diffusion with the network in its prologue; needs ``--weights``).
+(the diffusion with the network in its prologue; needs ``--weights``),
+tet_convec / tet_diffu (fem_convec / fem_diffu on the reference driver's
+disconnected tetrahedra over the case's nodes).
 """
 import argparse
 
@@ -39,6 +41,7 @@ def main(argv=None):
     dev = workload.DeviceCase(workload.HostCase(cfg))
     out64 = None
     mlp = None
+    tet = None
     calls = []
     for k in a.kernels.split(","):
         if k == "convec":
@@ -51,6 +54,10 @@ def main(argv=None):
                               for n in (1, 3, 1))
             fn = dev.convec_mixed if k == "convec_mixed" else dev.diffu_mixed
             calls.append(lambda fn=fn: fn(a.precision, out=out64))
+        elif k in ("tet_convec", "tet_diffu"):
+            if tet is None:
+                tet = workload.TetCase(dev.host)
+            calls.append(tet.convec if k == "tet_convec" else tet.diffu)
         elif k == "estimator":
             calls.append(lambda: learn.entropy_viscosity(dev))
         elif k in ("learned", "diffu_learned"):

@@ -188,3 +188,72 @@ class DeviceCase:
                                    self.mu_fluid, self.mu_e, self.mu_sgs, self.Dmass, self.Dmom, self.Dener,
                                    stream=stream)
         return self.Dmass, self.Dmom, self.Dener
+
+
+class TetCase:
+    """The reference driver's TET04 data (main.f90:365-407) on the GPU.
+
+    Disconnected unit tetrahedra (gen_tet_mesh): npoin_t = 4 nelem_t nodes,
+    taken as the first multiple of 4 of a hex workload's nodes, whose node
+    fields the tet kernels read (the driver passes the same u, q, rho, pr, E,
+    Tem, mu_fluid to its hex and tet kernels); mu_e = mu_sgs = 1
+    (main.f90:402-406); metric by tet_jacobian on the device.
+    """
+
+    def __init__(self, host, device="cuda", dtype=None):
+        import torch
+
+        from . import kernels
+
+        dtype = dtype or torch.float32
+        np_dt = np.float32 if dtype == torch.float32 else np.float64
+        dev = torch.device(device)
+        self.dtype = dtype
+        self.npoin = (host.npoin // 4) * 4
+        self.nelem = self.npoin // 4
+        t = fem.tet_element_tables(np_dt)
+        connec, coord, _ = fem.tet_mesh_disconnected(self.nelem)
+
+        def up(a, dt=None):
+            return torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
+
+        self.connec = up(connec)
+        self.Ngp, self.dNgp = up(t["Ngp"]), up(t["dNgp"])
+        c = up(coord, dtype)
+        self.He = torch.empty(36 * self.nelem, dtype=dtype, device=dev)
+        self.gpvol = torch.empty(4 * self.nelem, dtype=dtype, device=dev)
+        kernels.tet_jacobian(self.nelem, self.npoin, self.connec, c, self.dNgp, up(t["wgp"]), self.gpvol, self.He)
+        del c
+        f, n, m = host.fields, self.npoin, host.npoin
+        for k in ("rho", "pr", "E", "Tem", "mu_fluid"):
+            setattr(self, k, up(f[k][:n], dtype))
+        for k in ("u", "q"):
+            setattr(self, k, up(f[k].reshape(3, m)[:, :n].reshape(-1), dtype))
+        self.mu_e = torch.ones(4 * self.nelem, dtype=dtype, device=dev)
+        self.mu_sgs = torch.ones(4 * self.nelem, dtype=dtype, device=dev)
+        self.Cp, self.Pr = 1.0, 1.0  # main.f90:412-413
+        self.R = tuple(torch.empty(k * n, dtype=dtype, device=dev) for k in (1, 3, 1))
+        self.D = tuple(torch.empty(k * n, dtype=dtype, device=dev) for k in (1, 3, 1))
+
+    def convec(self, stream=None):
+        from . import kernels
+
+        kernels.fem_convec(self.nelem, self.npoin, self.connec, self.Ngp, self.dNgp, self.He, self.gpvol, self.u,
+                           self.q, self.rho, self.pr, self.E, *self.R, stream=stream)
+        return self.R
+
+    def diffu(self, stream=None):
+        from . import kernels
+
+        kernels.fem_diffu(self.nelem, self.npoin, self.connec, self.Ngp, self.dNgp, self.He, self.gpvol, self.Cp,
+                          self.Pr, self.rho, self.u, self.Tem, self.mu_fluid, self.mu_e, self.mu_sgs, *self.D,
+                          stream=stream)
+        return self.D
+
+    # Algorithmic bytes per element: connec 16, He 144, gpvol 16, node fields
+    # (convection: u, q, rho, pr, E = 9 values; diffusion: rho, u, Tem, mu_fluid
+    # = 6 values and mu_e, mu_sgs 2 x 4 per element) and 5 residuals per node,
+    # every value read or written once.
+    def algorithmic_bytes(self, which):
+        reals = 36 + 4 + (4 * 9 if which == "convec" else 4 * 6 + 2 * 4) + 4 * 5
+        return self.nelem * (4 * 4 + reals * self.dtype.itemsize)

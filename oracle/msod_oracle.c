@@ -401,12 +401,12 @@ void F(orc_element_basis)(int P, const int *AtoIJK, const real *xgp,
     free(dN);
 }
 
-/* elem_jacobian, jacobian_oper.f90:7-136 (3-D branch): Je = dNgp . x, cofactor
- * inverse He = Je^-1, gpvol = wgp * det(Je). */
-void F(orc_elem_jacobian)(int P, int nelem, int npoin, const int *connec, const real *coord,
-                          const real *dNgp, const real *wgp, real *gpvol, real *He)
+/* elem_jacobian, jacobian_oper.f90:7-136 (3-D branch), and tet_jacobian,
+ * jacobian_oper.f90:138-267 (the same steps for n = 4): Je = dNgp . x,
+ * cofactor inverse He = Je^-1, gpvol = wgp * det(Je); n nodes = n points. */
+static void jacobian_n(int n, int nelem, int npoin, const int *connec, const real *coord, const real *dNgp,
+                       const real *wgp, real *gpvol, real *He)
 {
-    int Q = P + 1, n = Q * Q * Q;
     for (int64_t e = 0; e < nelem; ++e) {
         for (int g = 0; g < n; ++g) {
             real Je[3][3];
@@ -444,6 +444,13 @@ void F(orc_elem_jacobian)(int P, int nelem, int npoin, const int *connec, const 
             gpvol[(int64_t)e * n + g] = wgp[g] * det;
         }
     }
+}
+
+void F(orc_elem_jacobian)(int P, int nelem, int npoin, const int *connec, const real *coord,
+                          const real *dNgp, const real *wgp, real *gpvol, real *He)
+{
+    int Q = P + 1;
+    jacobian_n(Q * Q * Q, nelem, npoin, connec, coord, dNgp, wgp, gpvol, He);
 }
 
 /* create_mesh, mod_mesh.f90:11-65: disconnected mesh, connec = (e-1)*n+a,
@@ -1151,5 +1158,204 @@ int F(orc_entropy_viscosity)(int P, int nelem, int npoin, const int *connec, con
         if (numax_out) numax_out[e] = numax;
     }
     free(eta); free(ul); free(rl);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Linear tetrahedra: elem_tet.f90, quadrature_rules.f90:84-99,              */
+/* mod_mesh.f90:71-126, jacobian_oper.f90:138-267, elem_convec.f90:839-948,  */
+/* elem_diffu.f90:199-317.  Layouts (E = nelem):                             */
+/*   connec(nelem,4) connec[a*E+e]; He(3,3,4,nelem) He[((e*4+g)*3+j)*3+i];   */
+/*   gpvol(1,4,nelem) gpvol[e*4+g]; Ngp(4,4) Ngp[c*4+r] for Ngp(r,c);       */
+/*   dNgp(3,4,4) dNgp[(g*4+a)*3+d]; mu_e(nelem,4) mu_e[a*E+e].               */
+/* ------------------------------------------------------------------------- */
+
+/* tet_4points (quadrature_rules.f90:84-99) and tet_04 (elem_tet.f90:9-36) at
+ * each point, as the driver fills its tables (main.f90:377-383):
+ * Ngp(igaus,inode) = N_inode(x_igaus), dNgp(:,inode,igaus) = dN_inode. */
+void F(orc_tet_element_tables)(real *Ngp, real *dNgp, real *xgp, real *wgp)
+{
+    const real a = (real)0.5854101966249680, b = (real)0.1381966011250110;
+    const real X[4][3] = {{a, b, b}, {b, a, b}, {b, b, a}, {b, b, b}};
+    for (int g = 0; g < 4; ++g) {
+        for (int d = 0; d < 3; ++d) xgp[d * 4 + g] = X[g][d];
+        wgp[g] = (real)0.25;
+    }
+    for (int g = 0; g < 4; ++g) {
+        const real xi = xgp[0 * 4 + g], eta = xgp[1 * 4 + g], zeta = xgp[2 * 4 + g];
+        const real N[4] = {(real)1.0 - xi - eta - zeta, xi, eta, zeta};
+        const real dN[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        for (int i = 0; i < 4; ++i) {
+            Ngp[i * 4 + g] = N[i];
+            for (int d = 0; d < 3; ++d) dNgp[(g * 4 + i) * 3 + d] = dN[i][d];
+        }
+    }
+}
+
+/* gen_tet_mesh (mod_mesh.f90:71-126): connec(e,a) = (e-1)*4 + a, every
+ * element a copy of xyzBase(4,3) (xyzBase[d*4+a]) shifted by 3.0 per element. */
+void F(orc_gen_tet_mesh)(int nelem, int npoin, const real *xyzBase, int *connec, real *coord)
+{
+    for (int64_t e = 0; e < nelem; ++e)
+        for (int a = 0; a < 4; ++a) connec[(int64_t)a * nelem + e] = (int)(e * 4 + a + 1);
+    real xyz0 = (real)0.0;
+    for (int64_t e = 0; e < nelem; ++e) {
+        for (int a = 0; a < 4; ++a) {
+            int64_t p = connec[(int64_t)a * nelem + e] - 1;
+            for (int d = 0; d < 3; ++d) coord[(int64_t)d * npoin + p] = xyzBase[d * 4 + a] + xyz0;
+        }
+        xyz0 = xyz0 + (real)3.0;
+    }
+}
+
+void F(orc_tet_jacobian)(int nelem, int npoin, const int *connec, const real *coord, const real *dNgp,
+                         const real *wgp, real *gpvol, real *He)
+{
+    jacobian_n(4, nelem, npoin, connec, coord, dNgp, wgp, gpvol, He);
+}
+
+/* gpcar(inode,idime) = DOT_PRODUCT(He(idime,:,igaus,ielem), dNgp(:,inode,igaus)). */
+static void tet_gpcar(const real *He, const real *dNgp, int64_t e, int g, real gpcar[4][3])
+{
+    const real *H = He + ((int64_t)e * 4 + g) * 9;
+    for (int id = 0; id < 3; ++id)
+        for (int a = 0; a < 4; ++a) {
+            real dot = (real)0.0;
+            for (int j = 0; j < 3; ++j) dot = dot + H[j * 3 + id] * dNgp[(g * 4 + a) * 3 + j];
+            gpcar[a][id] = dot;
+        }
+}
+
+/* fem_convec, elem_convec.f90:839-948. */
+int F(orc_fem_convec)(int nelem, int npoin, const int *connec, const real *Ngp, const real *dNgp, const real *He,
+                      const real *gpvol, const real *u, const real *q, const real *rho, const real *pr,
+                      const real *E, real *Rmass, real *Rmom, real *Rener, int nthreads)
+{
+    const int64_t np = npoin;
+    memset(Rmass, 0, sizeof(real) * np);
+    memset(Rmom, 0, sizeof(real) * 3 * np);
+    memset(Rener, 0, sizeof(real) * np);
+    const int atomic = nthreads > 1;
+    const real half = (real)0.5;
+#pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) if (atomic) schedule(static, 1024)
+    for (int64_t e = 0; e < nelem; ++e) {
+        int64_t ip[4];
+        for (int a = 0; a < 4; ++a) ip[a] = connec[(int64_t)a * nelem + e] - 1;
+        real Re_mass[4] = {0, 0, 0, 0}, Re_ener[4] = {0, 0, 0, 0}, Re_mom[4][3] = {{0}};
+        for (int g = 0; g < 4; ++g) {
+            real divQ = 0, divFe = 0, gradRho[3] = {0, 0, 0}, gradE[3] = {0, 0, 0}, gradP[3] = {0, 0, 0};
+            real gradU[3][3] = {{0}}, divF[3] = {0, 0, 0};
+            real gpcar[4][3];
+            tet_gpcar(He, dNgp, e, g, gpcar);
+            for (int id = 0; id < 3; ++id)
+                for (int j = 0; j < 4; ++j) {
+                    const int64_t p = ip[j];
+                    const real Ep = E[p] + pr[p];
+                    divQ = divQ + gpcar[j][id] * q[id * np + p];
+                    divFe = divFe + gpcar[j][id] * Ep * u[id * np + p];
+                    gradRho[id] = gradRho[id] + gpcar[j][id] * rho[p];
+                    gradE[id] = gradE[id] + gpcar[j][id] * Ep;
+                    gradP[id] = gradP[id] + gpcar[j][id] * pr[p];
+                    for (int jd = 0; jd < 3; ++jd) {
+                        gradU[id][jd] = gradU[id][jd] + gpcar[j][jd] * u[id * np + p];
+                        divF[id] = divF[id] + gpcar[j][jd] * q[id * np + p] * u[jd * np + p];
+                    }
+                }
+            const real divU = gradU[0][0] + gradU[1][1] + gradU[2][2];
+            for (int a = 0; a < 4; ++a) {
+                const int64_t p = ip[a];
+                real aux1 = 0, aux2 = 0;
+                for (int id = 0; id < 3; ++id) {
+                    aux1 = aux1 + gradRho[id] * u[id * np + p];
+                    aux2 = aux2 + gradE[id] * u[id * np + p];
+                }
+                const real w = gpvol[e * 4 + g] * Ngp[a * 4 + g] * half;
+                Re_mass[a] = Re_mass[a] + w * (divQ + rho[p] * divU + aux1);
+                Re_ener[a] = Re_ener[a] + w * (divFe + (E[p] + pr[p]) * divU + aux2);
+                for (int id = 0; id < 3; ++id) {
+                    real aux3 = 0, aux4 = 0;
+                    for (int jd = 0; jd < 3; ++jd) {
+                        aux3 = aux3 + gradU[id][jd] * q[jd * np + p];
+                        aux4 = aux4 + u[id * np + p] * u[jd * np + p] * gradRho[jd];
+                    }
+                    Re_mom[a][id] = Re_mom[a][id] + w * (divF[id] + q[id * np + p] * divU + aux3 + aux4 + gradP[id]);
+                }
+            }
+        }
+        for (int a = 0; a < 4; ++a) {
+            SCATTER(Rmass, ip[a], Re_mass[a], atomic);
+            SCATTER(Rener, ip[a], Re_ener[a], atomic);
+            for (int d = 0; d < 3; ++d) SCATTER(Rmom, d * np + ip[a], Re_mom[a][d], atomic);
+        }
+    }
+    return 0;
+}
+
+/* fem_diffu, elem_diffu.f90:199-317.  It reads Ngp(inode,igaus) -- the
+ * transpose of fem_convec's Ngp(igaus,inode) -- and kappa with c_ener mu_e /
+ * 0.4; c_rho = c_ener = 1 (mod_numerical_params.f90:26-27).  Its assembly has
+ * no atomics (:306-312); the threaded oracle adds atomically. */
+int F(orc_fem_diffu)(int nelem, int npoin, const int *connec, const real *Ngp, const real *dNgp, const real *He,
+                     const real *gpvol, real Cp, real Pr, const real *rho, const real *u, const real *Tem,
+                     const real *mu_fluid, const real *mu_e, const real *mu_sgs, real *Rmass, real *Rmom,
+                     real *Rener, int nthreads)
+{
+    const int64_t np = npoin;
+    memset(Rmass, 0, sizeof(real) * np);
+    memset(Rmom, 0, sizeof(real) * 3 * np);
+    memset(Rener, 0, sizeof(real) * np);
+    const int atomic = nthreads > 1;
+    const real c_rho = (real)1.0, c_ener = (real)1.0;
+#pragma omp parallel for num_threads(nthreads > 0 ? nthreads : 1) if (atomic) schedule(static, 1024)
+    for (int64_t e = 0; e < nelem; ++e) {
+        int64_t ip[4];
+        for (int a = 0; a < 4; ++a) ip[a] = connec[(int64_t)a * nelem + e] - 1;
+        real Re_mass[4] = {0, 0, 0, 0}, Re_ener[4] = {0, 0, 0, 0}, Re_mom[4][3] = {{0}};
+        for (int g = 0; g < 4; ++g) {
+            real auxRho = 0, auxNu = 0, auxMu = 0, auxKappa = 0;
+            for (int a = 0; a < 4; ++a) auxRho = auxRho + Ngp[g * 4 + a] * rho[ip[a]];
+            for (int a = 0; a < 4; ++a) {
+                const real me = mu_e[(int64_t)a * nelem + e], ms = mu_sgs[(int64_t)a * nelem + e];
+                const real mf = mu_fluid[ip[a]];
+                auxNu = auxNu + Ngp[g * 4 + a] * me * (c_rho / auxRho);
+                auxMu = auxMu + Ngp[g * 4 + a] * (mf + auxRho * ms + me);
+                auxKappa = auxKappa + Ngp[g * 4 + a] * (mf * (Cp / Pr) + c_ener * me / (real)0.4 + auxRho * ms / (real)0.9);
+            }
+            real gpcar[4][3];
+            tet_gpcar(He, dNgp, e, g, gpcar);
+            real gradRho[3] = {0, 0, 0}, gradT[3] = {0, 0, 0}, gradU[3][3] = {{0}};
+            for (int id = 0; id < 3; ++id)
+                for (int a = 0; a < 4; ++a) {
+                    const int64_t p = ip[a];
+                    gradRho[id] = gradRho[id] + gpcar[a][id] * rho[p];
+                    gradT[id] = gradT[id] + gpcar[a][id] * Tem[p];
+                    for (int jd = 0; jd < 3; ++jd) gradU[id][jd] = gradU[id][jd] + gpcar[a][id] * u[jd * np + p];
+                }
+            const real divU = gradU[0][0] + gradU[1][1] + gradU[2][2];
+            real tau[3][3] = {{0}}, tauU[3] = {0, 0, 0};
+            for (int id = 0; id < 3; ++id) {
+                tau[id][id] = -((real)2.0 / (real)3.0 * divU);
+                for (int jd = 0; jd < 3; ++jd) tau[id][jd] = tau[id][jd] + gradU[id][jd] + gradU[jd][id];
+            }
+            for (int jd = 0; jd < 3; ++jd) {
+                real auxU = 0;
+                for (int a = 0; a < 4; ++a) auxU = auxU + Ngp[g * 4 + a] * u[jd * np + ip[a]];
+                for (int id = 0; id < 3; ++id) tauU[id] = tauU[id] + tau[id][jd] * auxU;
+            }
+            const real gv = gpvol[e * 4 + g];
+            for (int id = 0; id < 3; ++id)
+                for (int a = 0; a < 4; ++a) {
+                    Re_mass[a] = Re_mass[a] + gv * auxNu * gpcar[a][id] * gradRho[id];
+                    Re_ener[a] = Re_ener[a] + gv * gpcar[a][id] * (auxMu * tauU[id] + auxKappa * gradT[id]);
+                    for (int jd = 0; jd < 3; ++jd)
+                        Re_mom[a][id] = Re_mom[a][id] + gv * gpcar[a][jd] * auxMu * tau[id][jd];
+                }
+        }
+        for (int a = 0; a < 4; ++a) {
+            SCATTER(Rmass, ip[a], Re_mass[a], atomic);
+            SCATTER(Rener, ip[a], Re_ener[a], atomic);
+            for (int d = 0; d < 3; ++d) SCATTER(Rmom, d * np + ip[a], Re_mom[a][d], atomic);
+        }
+    }
     return 0;
 }

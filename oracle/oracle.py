@@ -201,3 +201,64 @@ def entropy_viscosity(P, nelem, npoin, geom, rho, u, pr, gamma=1.4, ce=0.1, cmax
     if rc != 0:
         raise RuntimeError("orc_entropy_viscosity failed")
     return mu_e, nu, numax
+
+
+# ---------------------------------------------------------------------------
+# Linear tetrahedra (elem_tet.f90, quadrature_rules.f90:84-99, mod_mesh.f90:71-126,
+# jacobian_oper.f90:138-267, elem_convec.f90:839-948, elem_diffu.f90:199-317)
+# ---------------------------------------------------------------------------
+
+def tet_element_tables(dtype=np.float32):
+    """Ngp(4,4) (Ngp[a*4+g] = N_a(x_g)), dNgp(3,4,4), xgp(4,3), wgp(4): main.f90:377-383."""
+    Ngp = np.zeros(16, dtype)
+    dNgp = np.zeros(48, dtype)
+    xgp = np.zeros(12, dtype)
+    wgp = np.zeros(4, dtype)
+    getattr(lib(), "orc_tet_element_tables" + _sfx(dtype))(_p(Ngp), _p(dNgp), _p(xgp), _p(wgp))
+    return dict(Ngp=Ngp, dNgp=dNgp, xgp=xgp, wgp=wgp)
+
+
+def gen_tet_mesh(nelem, xyzBase=None, dtype=np.float32):
+    """The driver's disconnected tet mesh: npoin = 4 nelem (main.f90:386-394)."""
+    if xyzBase is None:  # xyzTET, main.f90:390-393, as xyzBase[d*4+a]
+        xyzBase = np.array([0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1], dtype)
+    npoin = 4 * nelem
+    connec = np.zeros(4 * nelem, np.int32)
+    coord = np.zeros(3 * npoin, dtype)
+    getattr(lib(), "orc_gen_tet_mesh" + _sfx(dtype))(C.c_int(nelem), C.c_int(npoin), _p(_c(xyzBase, dtype)),
+                                                     _p(connec), _p(coord))
+    return connec, coord
+
+
+def tet_jacobian(nelem, npoin, connec, coord, dNgp, wgp, dtype=np.float32):
+    gpvol = np.zeros(4 * nelem, dtype)
+    He = np.zeros(36 * nelem, dtype)
+    getattr(lib(), "orc_tet_jacobian" + _sfx(dtype))(
+        C.c_int(nelem), C.c_int(npoin), _p(_c(connec, np.int32)), _p(_c(coord, dtype)), _p(_c(dNgp, dtype)),
+        _p(_c(wgp, dtype)), _p(gpvol), _p(He))
+    return He, gpvol
+
+
+def fem_convec(nelem, npoin, connec, Ngp, dNgp, He, gpvol, u, q, rho, pr, E, dtype=np.float32, nthreads=1):
+    ins = [_c(x, dtype) for x in (Ngp, dNgp, He, gpvol, u, q, rho, pr, E)]
+    out = [np.zeros(n * npoin, dtype) for n in (1, 3, 1)]
+    rc = getattr(lib(), "orc_fem_convec" + _sfx(dtype))(
+        C.c_int(nelem), C.c_int(npoin), _p(_c(connec, np.int32)), *[_p(x) for x in ins], *[_p(x) for x in out],
+        C.c_int(nthreads))
+    if rc != 0:
+        raise RuntimeError("orc_fem_convec failed")
+    return tuple(out)
+
+
+def fem_diffu(nelem, npoin, connec, Ngp, dNgp, He, gpvol, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs,
+              dtype=np.float32, nthreads=1):
+    a = [_c(x, dtype) for x in (Ngp, dNgp, He, gpvol)]
+    b = [_c(x, dtype) for x in (rho, u, Tem, mu_fluid, mu_e, mu_sgs)]
+    out = [np.zeros(n * npoin, dtype) for n in (1, 3, 1)]
+    real = C.c_float if np.dtype(dtype) == np.float32 else C.c_double
+    rc = getattr(lib(), "orc_fem_diffu" + _sfx(dtype))(
+        C.c_int(nelem), C.c_int(npoin), _p(_c(connec, np.int32)), *[_p(x) for x in a], real(Cp), real(Pr),
+        *[_p(x) for x in b], *[_p(x) for x in out], C.c_int(nthreads))
+    if rc != 0:
+        raise RuntimeError("orc_fem_diffu failed")
+    return tuple(out)

@@ -149,3 +149,118 @@ def lumped_mass(geom, nelem, npoin, n):
     nodes = geom["connec"].reshape(n, nelem).T - 1
     np.add.at(M, nodes, geom["gpvol"].astype(np.float64).reshape(nelem, n))
     return M
+
+
+# ---------------------------------------------------------------------------
+# Linear tetrahedra (elem_convec.f90:839-948, elem_diffu.f90:199-317), whole
+# mesh at once with einsum; arrays as in the C oracle (flattened Fortran).
+# ---------------------------------------------------------------------------
+
+def _tet_gather(nelem, npoin, connec, Ngp, dNgp, He, gpvol):
+    con = np.asarray(connec).reshape(4, nelem).T - 1                   # [e, a]
+    H = np.asarray(He, np.float64).reshape(nelem, 4, 3, 3)             # [e, g, j, i] = He(i,j,g,e)
+    dN = np.asarray(dNgp, np.float64).reshape(4, 4, 3)                 # [g, a, j]
+    gpcar = np.einsum("egji,gaj->egai", H, dN)                         # [e, g, a, i]
+    gv = np.asarray(gpvol, np.float64).reshape(nelem, 4)               # [e, g]
+    Nf = np.asarray(Ngp, np.float64).reshape(4, 4)                     # Nf[c, r] = Ngp(r, c)
+    return con, gpcar, gv, Nf
+
+
+def _vec(x, npoin, con):
+    return np.asarray(x, np.float64).reshape(3, npoin).T[con]           # [e, a, i]
+
+
+def _tet_scatter(con, npoin, Rm, Rq, Re):
+    Rmass = np.zeros(npoin)
+    Rener = np.zeros(npoin)
+    Rmom = np.zeros((3, npoin))
+    np.add.at(Rmass, con, Rm)
+    np.add.at(Rener, con, Re)
+    for i in range(3):
+        np.add.at(Rmom[i], con, Rq[..., i])
+    return Rmass, Rmom.reshape(-1), Rener
+
+
+def fem_convec(nelem, npoin, connec, Ngp, dNgp, He, gpvol, u, q, rho, pr, E):
+    con, gc, gv, Nf = _tet_gather(nelem, npoin, connec, Ngp, dNgp, He, gpvol)
+    U, Qv = _vec(u, npoin, con), _vec(q, npoin, con)
+    r = np.asarray(rho, np.float64)[con]
+    p = np.asarray(pr, np.float64)[con]
+    Ep = np.asarray(E, np.float64)[con] + p
+    divQ = np.einsum("egai,eai->eg", gc, Qv)
+    divFe = np.einsum("egai,ea,eai->eg", gc, Ep, U)
+    gR = np.einsum("egai,ea->egi", gc, r)
+    gE = np.einsum("egai,ea->egi", gc, Ep)
+    gP = np.einsum("egai,ea->egi", gc, p)
+    gU = np.einsum("egaj,eai->egij", gc, U)                            # d u_i / d x_j
+    divF = np.einsum("egaj,eai,eaj->egi", gc, Qv, U)
+    divU = np.einsum("egii->eg", gU)
+    w = gv[:, :, None] * Nf.T[None, :, :] * 0.5                       # [e, g, a]: Ngp(igaus, inode)
+    aux1 = np.einsum("egi,eai->ega", gR, U)
+    aux2 = np.einsum("egi,eai->ega", gE, U)
+    Rm = np.einsum("ega,ega->ea", w, divQ[:, :, None] + r[:, None, :] * divU[:, :, None] + aux1)
+    Re = np.einsum("ega,ega->ea", w, divFe[:, :, None] + Ep[:, None, :] * divU[:, :, None] + aux2)
+    aux3 = np.einsum("egij,eaj->egai", gU, Qv)
+    aux4 = np.einsum("eai,eaj,egj->egai", U, U, gR)
+    mom = divF[:, :, None, :] + Qv[:, None, :, :] * divU[:, :, None, None] + aux3 + aux4 + gP[:, :, None, :]
+    Rq = np.einsum("ega,egai->eai", w, mom)
+    return _tet_scatter(con, npoin, Rm, Rq, Re)
+
+
+def fem_diffu(nelem, npoin, connec, Ngp, dNgp, He, gpvol, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs):
+    con, gc, gv, Nf = _tet_gather(nelem, npoin, connec, Ngp, dNgp, He, gpvol)
+    N2 = Nf                                                            # N2[g, a] = Ngp(inode=a, igaus=g)
+    U = _vec(u, npoin, con)
+    r = np.asarray(rho, np.float64)[con]
+    T = np.asarray(Tem, np.float64)[con]
+    mf = np.asarray(mu_fluid, np.float64)[con]
+    me = np.asarray(mu_e, np.float64).reshape(4, nelem).T
+    ms = np.asarray(mu_sgs, np.float64).reshape(4, nelem).T
+    aRho = np.einsum("ga,ea->eg", N2, r)
+    aNu = np.einsum("ga,ea->eg", N2, me) / aRho
+    aMu = np.einsum("ga,ega->eg", N2, mf[:, None, :] + aRho[:, :, None] * ms[:, None, :] + me[:, None, :])
+    aKap = np.einsum("ga,ega->eg", N2, mf[:, None, :] * (Cp / Pr) + me[:, None, :] / 0.4
+                     + aRho[:, :, None] * ms[:, None, :] / 0.9)
+    gR = np.einsum("egai,ea->egi", gc, r)
+    gT = np.einsum("egai,ea->egi", gc, T)
+    gU = np.einsum("egai,eaj->egij", gc, U)                            # gradU(i,j) = d u_j / d x_i
+    divU = np.einsum("egii->eg", gU)
+    tau = gU + np.swapaxes(gU, 2, 3) - (2.0 / 3.0) * divU[:, :, None, None] * np.eye(3)
+    aU = np.einsum("ga,eaj->egj", N2, U)
+    tauU = np.einsum("egij,egj->egi", tau, aU)
+    Rm = np.einsum("eg,egai,egi->ea", gv * aNu, gc, gR)
+    Re = np.einsum("eg,egai,egi->ea", gv, gc, aMu[:, :, None] * tauU + aKap[:, :, None] * gT)
+    Rq = np.einsum("eg,egaj,egij->eai", gv * aMu, gc, tau)
+    return _tet_scatter(con, npoin, Rm, Rq, Re)
+
+
+def tet_mesh_shared(n, jitter=0.0, seed=0):
+    """Shared-node tet mesh of an n^3 grid of cubes of the unit cube: six
+    tetrahedra per cube around its main diagonal (Kuhn), interior vertices
+    jittered.  Returns (connec[a*E+e] 1-based int32, coord[d*npoin+p] float32, nelem, npoin)."""
+    m = n + 1
+    g = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing="ij"), -1).reshape(-1, 3).astype(np.float64) / n
+    rng = np.random.default_rng(seed)
+    inner = np.all((g > 0) & (g < 1), axis=1)
+    g[inner] += jitter / n * rng.uniform(-1, 1, (int(inner.sum()), 3))
+    vid = lambda i, j, k: (i * m + j) * m + k
+    tets = []
+    perms = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    for i in range(n):
+        for j in range(n):
+            for k in range(n):
+                for pm in perms:
+                    c = [i, j, k]
+                    t = [vid(*c)]
+                    for ax in pm:
+                        c = list(c)
+                        c[ax] += 1
+                        t.append(vid(*c))
+                    if pm in ((0, 2, 1), (1, 0, 2), (2, 1, 0)):  # odd permutation: positive orientation
+                        t[1], t[2] = t[2], t[1]
+                    tets.append(t)
+    tets = np.array(tets, np.int64)
+    nelem, npoin = len(tets), m ** 3
+    connec = (tets.T.reshape(-1) + 1).astype(np.int32)
+    coord = g.T.reshape(-1).astype(np.float32)
+    return connec, coord, nelem, npoin
