@@ -250,6 +250,16 @@ int msod_mesh_structured(int porder, int nx, int ny, int nz, const int *AtoI, co
                          const int *AtoK, double jitter, uint64_t seed, int *connec,
                          float *coord);
 
+/* Host: the reference driver's own case.  create_mesh (mod_mesh.f90:11-65):
+ * disconnected elements, connec(e,a) = (e-1)*nnode + a, element e = xyzBase
+ * (xyzBase[d*nnode+a]; the driver passes xgp) shifted by 3(e-1) along every
+ * axis; npoin = nelem*nnode; coord may be NULL.  msod_reference_ic: the driver's
+ * initial condition (main.f90:320-361), FP32, mu_e = mu_sgs = mu_fluid = 1. */
+int msod_mesh_disconnected(int porder, int nelem, const float *xyzBase, int *connec, float *coord);
+int msod_reference_ic(int porder, int nelem, int64_t npoin, const int *connec, float *u, float *q,
+                      float *rho, float *pr, float *E, float *Tem, float *mu_fluid, float *mu_e,
+                      float *mu_sgs);
+
 /* Host: seeded node fields (FP32) for recipe `kind` with `nmodes` Fourier
  * modes per velocity component: rho, u(npoin,3), q = rho u, pr,
  * E = pr/(gamma-1)/rho + |u|^2/2, Tem = pr/(rho Rgas), mu_fluid = 1.8e-5

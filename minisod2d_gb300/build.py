@@ -37,6 +37,7 @@ def sources():
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     files.append(os.path.join(INCLUDE, "msod.h"))
+    files.append(os.path.join(HERE, "driver", "msod_driver.cpp"))
     return files
 
 
@@ -48,7 +49,7 @@ def _compile(args):
 
 def build(force=False, verbose=False, ptxas_verbose=False):
     """Compile libmsod.so if any source is newer than it.  Returns its path."""
-    if not force and os.path.exists(LIB):
+    if not force and os.path.exists(LIB) and os.path.exists(os.path.join(HERE, "msod_driver")):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(f) <= t for f in _deps()):
             return LIB
@@ -86,7 +87,26 @@ def build(force=False, verbose=False, ptxas_verbose=False):
         print(r.stdout + r.stderr)
         raise RuntimeError("libmsod link failed")
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
+
+
+DRIVER_SRC = os.path.join(HERE, "driver", "msod_driver.cpp")
+DRIVER = os.path.join(HERE, "msod_driver")
+
+
+def build_driver():
+    """The benchmark driver executable (main.f90 on the C ABI), linked to libmsod.so."""
+    tmp = DRIVER + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I" + INCLUDE, DRIVER_SRC, "-L" + HERE, "-lmsod",
+           "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        print(" ".join(cmd))
+        print(r.stdout + r.stderr)
+        raise RuntimeError("msod_driver build failed")
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":

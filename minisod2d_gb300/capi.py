@@ -72,6 +72,8 @@ SIGNATURES = {
     "msod_fem_element_tables_f64": [_i] + [_p] * 10,
     "msod_mesh_structured": [_i, _i, _i, _i, _p, _p, _p, _d, _u64, _p, _p],
     "msod_fields_recipe": [_i, _i, _u64, _i64, _p, _p, _p, _p, _p, _p, _p, _p],
+    "msod_mesh_disconnected": [_i, _i, _p, _p, _p],
+    "msod_reference_ic": [_i, _i, _i64] + [_p] * 10,
     "msod_entropy_viscosity": [_i, _i, _i] + [_p] * 8 + [_p, _p, _p, _f, _f, _f, _i, _p, _p, _p, _p],
     "msod_mlp_features": [_i, _i, _i] + [_p] * 8 + [_p, _p, _p, _f, _f, _f, _p, _p, _p],
     "msod_mlp_create": [C.POINTER(_p), _u64],

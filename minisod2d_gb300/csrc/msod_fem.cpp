@@ -491,4 +491,74 @@ int msod_tet_mesh_disconnected(int nelem, const float *xyzBase, int *connec, flo
     return MSOD_OK;
 }
 
+
+int msod_mesh_disconnected(int porder, int nelem, const float *xyzBase, int *connec, float *coord)
+{
+    // create_mesh (mod_mesh.f90:11-65): connec(e,a) = (e-1) n + a; element e is
+    // xyzBase(nnode,3) (xyzBase[d*n+a], the driver passes xgp) shifted by
+    // 3 (e-1) along every axis.
+    const int P = porder;
+    if (P < 1 || P > MSOD_MAX_PORDER) return msod::set_error(MSOD_ERR_PORDER, "porder %d", P);
+    const int n = (P + 1) * (P + 1) * (P + 1);
+    if (nelem < 1 || (int64_t)nelem * n >= ((int64_t)1 << 31))
+        return msod::set_error(MSOD_ERR_INVALID_ARG, "nelem*nnode must be in 1..2^31-1");
+    if (!connec || (coord && !xyzBase)) return msod::set_error(MSOD_ERR_INVALID_ARG, "NULL array");
+    const int64_t npoin = (int64_t)nelem * n;
+    for (int64_t e = 0; e < nelem; ++e)
+        for (int a = 0; a < n; ++a) connec[(int64_t)a * nelem + e] = (int)(e * n + a + 1);
+    if (!coord) return MSOD_OK;
+    float shift = 0.0f;
+    for (int64_t e = 0; e < nelem; ++e) {
+        for (int a = 0; a < n; ++a)
+            for (int d = 0; d < 3; ++d) coord[(int64_t)d * npoin + e * n + a] = xyzBase[d * n + a] + shift;
+        shift = shift + 3.0f;
+    }
+    return MSOD_OK;
+}
+
+int msod_reference_ic(int porder, int nelem, int64_t npoin, const int *connec, float *u, float *q, float *rho,
+                      float *pr, float *E, float *Tem, float *mu_fluid, float *mu_e, float *mu_sgs)
+{
+    // The driver's initial condition (main.f90:320-361): every field 1; nodes 1
+    // and 4 of every element get u = 10 / 20, rho = 10 / 20, pr = 100 / 200;
+    // then q = rho u, E = rho pr / ((gamma-1) rho) + q.u / 2, T = pr / (rho Rgas)
+    // with gamma = 1.4, Rgas = 287 (main.f90:52), in the driver's operation order.
+    const int P = porder;
+    if (P < 1 || P > MSOD_MAX_PORDER) return msod::set_error(MSOD_ERR_PORDER, "porder %d", P);
+    const int n = (P + 1) * (P + 1) * (P + 1);
+    if (nelem < 1 || npoin < 1) return msod::set_error(MSOD_ERR_INVALID_ARG, "nelem and npoin must be positive");
+    if (!connec || !u || !q || !rho || !pr || !E || !Tem || !mu_fluid || !mu_e || !mu_sgs)
+        return msod::set_error(MSOD_ERR_INVALID_ARG, "NULL array");
+    const float gamma = 1.4f, Rgas = 287.0f;
+    for (int64_t p = 0; p < npoin; ++p) {
+        for (int d = 0; d < 3; ++d) u[d * npoin + p] = 1.0f;
+        rho[p] = pr[p] = E[p] = Tem[p] = mu_fluid[p] = 1.0f;
+    }
+    for (int64_t i = 0; i < (int64_t)nelem * n; ++i) mu_e[i] = mu_sgs[i] = 1.0f;
+    for (int64_t e = 0; e < nelem; ++e) {
+        const int64_t a = connec[e] - 1, b = connec[3 * (int64_t)nelem + e] - 1;  // nodes 1 and 4
+        if (a < 0 || a >= npoin || b < 0 || b >= npoin)
+            return msod::set_error(MSOD_ERR_INVALID_ARG, "connec entry outside 1..npoin");
+        for (int d = 0; d < 3; ++d) {
+            u[d * npoin + a] = 10.0f;
+            u[d * npoin + b] = 20.0f;
+        }
+        rho[a] = 10.0f;
+        rho[b] = 20.0f;
+        pr[a] = 100.0f;
+        pr[b] = 200.0f;
+    }
+    for (int64_t p = 0; p < npoin; ++p) {
+        float fmag = 0.0f;
+        for (int d = 0; d < 3; ++d) {
+            q[d * npoin + p] = rho[p] * u[d * npoin + p];
+            fmag = fmag + q[d * npoin + p] * u[d * npoin + p];
+        }
+        const float eint = pr[p] / ((gamma - 1.0f) * rho[p]);
+        E[p] = rho[p] * eint + 0.5f * fmag;
+        Tem[p] = pr[p] / (rho[p] * Rgas);
+    }
+    return MSOD_OK;
+}
+
 }  // extern "C"

@@ -92,3 +92,29 @@ def tet_mesh_disconnected(nelem, xyzBase=TET_BASE, coords=True):
     base = np.ascontiguousarray(xyzBase, np.float32)
     capi.call("msod_tet_mesh_disconnected", int(nelem), _p(base), _p(connec), _p(coord) if coords else None)
     return connec, coord, 4 * nelem
+
+
+def mesh_disconnected(porder, nelem, tables, coords=True):
+    """The reference driver's disconnected mesh (create_mesh with xyzBase = xgp):
+    (connec[a*nelem+e], coord[d*npoin+p] or None, npoin = nelem*nnode)."""
+    n = (int(porder) + 1) ** 3
+    connec = np.zeros(nelem * n, np.int32)
+    coord = np.zeros(3 * nelem * n, np.float32) if coords else None
+    xgp = np.ascontiguousarray(tables["xgp"], np.float32)
+    capi.call("msod_mesh_disconnected", int(porder), int(nelem), _p(xgp), _p(connec),
+              _p(coord) if coords else None)
+    return connec, coord, nelem * n
+
+
+def reference_ic(porder, nelem, npoin, connec):
+    """The reference driver's initial condition (main.f90:320-361) as FP32 arrays."""
+    n = (int(porder) + 1) ** 3
+    f = {k: np.zeros(npoin, np.float32) for k in ("rho", "pr", "E", "Tem", "mu_fluid")}
+    f["u"] = np.zeros(3 * npoin, np.float32)
+    f["q"] = np.zeros(3 * npoin, np.float32)
+    f["mu_e"] = np.ones(nelem * n, np.float32)
+    f["mu_sgs"] = np.ones(nelem * n, np.float32)
+    c = np.ascontiguousarray(connec, np.int32)
+    capi.call("msod_reference_ic", int(porder), int(nelem), int(npoin), _p(c), _p(f["u"]), _p(f["q"]), _p(f["rho"]),
+              _p(f["pr"]), _p(f["E"]), _p(f["Tem"]), _p(f["mu_fluid"]), _p(f["mu_e"]), _p(f["mu_sgs"]))
+    return f

@@ -1,0 +1,94 @@
+"""The benchmark driver (msod_driver, main.f90 on the C ABI) and the reference
+driver's own case (create_mesh, the initial condition of main.f90:320-361).
+
+CPU: the timers.dat / results_*.dat line formats (main.f90:499-500, :586-599)
+and the library's mesh and initial condition against the oracle, bit for bit.
+GPU: a small run of the driver: timers.dat, the results files against the
+FP64 oracle, the JSON summary.
+"""
+import json
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import refimpl as R
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DRIVER = os.path.join(os.path.dirname(HERE), "minisod2d_gb300", "msod_driver")
+
+
+def _driver():
+    from minisod2d_gb300 import build
+
+    build.build()
+    return DRIVER
+
+
+def test_driver_line_formats():
+    out = subprocess.run([_driver(), "--format-check"], capture_output=True, text=True, check=True).stdout
+    lines = out.splitlines()
+    # (i3,1x,4(f16.8,1x)): 3 + 4 x 17 columns, a blank after every value
+    assert lines[0] == "  7       0.00010690      12.50000000       0.00000000  123456.78901234 "
+    assert lines[1].startswith("*** ") and len(lines[1]) == 3 + 1 + 4 * 17
+    assert lines[2] == "1.0690000000000000E-004"
+    assert lines[3] == ("          42   1.00000000E+00  -2.49999994E-03   0.00000000E+00   3.00000000E+07"
+                        "  -1.00000000E+00")
+
+
+def test_driver_rejects_bad_options():
+    r = subprocess.run([_driver(), "--mesh", "spiral"], capture_output=True, text=True)
+    assert r.returncode == 2
+    r = subprocess.run([_driver(), "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 2
+
+
+@pytest.mark.parametrize("P", [2, 4])
+def test_reference_case_equals_the_oracle(P):
+    from minisod2d_gb300 import fem
+
+    t, ot = fem.element_tables(P), O.element_tables(P)
+    c, x, npoin = fem.mesh_disconnected(P, 11, t)
+    oc, ox = O.create_mesh_disconnected(P, 11, ot["xgp"])
+    assert np.array_equal(c, oc) and np.array_equal(x, ox)
+    f, of = fem.reference_ic(P, 11, npoin, c), O.reference_ic(P, 11, npoin, oc)
+    for k in f:
+        assert np.array_equal(f[k], of[k]), k
+
+
+@pytest.mark.gpu
+def test_driver_run_matches_the_oracle(cuda, tmp_path):
+    P, nelem, nruns = 4, 96, 3
+    r = subprocess.run([_driver(), "--porder", str(P), "--nelem", str(nelem), "--nruns", str(nruns), "--debug",
+                        "--out", str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "Avg. convective time" in r.stdout and "Basic TET results:" in r.stdout
+    rows = (tmp_path / "timers.dat").read_text().splitlines()
+    assert len(rows) == nruns
+    pat = re.compile(r"^[ \d]{3}( [ \d.]{15}\d){4} $")
+    assert all(pat.match(row) for row in rows), rows
+    assert all(float(v) > 0 for row in rows for v in row.split()[1:])
+    summary = json.loads((tmp_path / "results.json").read_text())
+    n = (P + 1) ** 3
+    assert summary["nelem"] == nelem and summary["npoin"] == nelem * n and summary["npoin_tet"] == nelem * n
+
+    # The results files against the FP64 oracle on the same case.
+    t = O.element_tables(P)
+    connec, coord = O.create_mesh_disconnected(P, nelem, t["xgp"])
+    npoin = nelem * n
+    f = O.reference_ic(P, nelem, npoin, connec)
+    He, gp = O.elem_jacobian(P, nelem, npoin, connec, coord, t["dNgp"], t["wgp"])
+    geom = dict(t, connec=connec, He=He, gpvol=gp)
+    ref_c = O.full_convec_ijk(P, nelem, npoin, geom, f["u"], f["q"], f["rho"], f["pr"], f["E"], dtype=np.float64,
+                              nthreads=8)
+    ref_d = O.full_diffusion_ijk(P, nelem, npoin, geom, 1.0, 1.0, f["rho"], f["u"], f["Tem"], f["mu_fluid"],
+                                 f["mu_e"], f["mu_sgs"], dtype=np.float64, nthreads=8)
+    for name, ref in (("results_convec.dat", ref_c), ("results_diffu.dat", ref_d)):
+        a = np.loadtxt(tmp_path / name)
+        assert a.shape == (npoin, 6) and np.array_equal(a[:, 0], np.arange(1, npoin + 1))
+        got = (a[:, 1], np.concatenate([a[:, 2], a[:, 3], a[:, 4]]), a[:, 5])
+        for g, r64 in zip(got, ref):
+            assert R.rel_l2(g, r64) < 1e-5, name
