@@ -31,6 +31,13 @@
  *  - `stream` is a cudaStream_t (NULL = the legacy default stream).  Kernel
  *    calls are asynchronous and stream-ordered; the host returns once the
  *    work is queued.
+ *  - Concurrency: the library keeps per-device state (the element tables of
+ *    the last call of each porder, the constant-bank derivative matrices of
+ *    each porder, the work buffers of the estimators and the learned
+ *    viscosity).  Kernel calls may overlap on different streams when calls of
+ *    the same porder pass the same element tables (dlxigp_ip, invAtoIJK,
+ *    gmshAtoI/J/K); calls of the viscosity estimators and the learned path must
+ *    not overlap one another.
  *  - Return value: MSOD_OK (0) or one of the MSOD_ERR_* codes below.  No
  *    entry point exits or traps; msod_last_error_string() describes the last
  *    failure of the calling thread.

@@ -25,22 +25,25 @@ thread_local char g_err[512] = "";
 std::atomic<int> g_checked{0};
 
 // Per-device library-owned device memory: the 4-byte flag word of
-// msod_check_element_tables and the per-call element tables of the kernels.
+// msod_check_element_tables and the per-call element tables of the kernels,
+// one table area per porder (calls of different porders on different streams
+// do not share one).
 std::mutex g_mu;
 int *g_flags[64] = {nullptr};
 TableScratch *g_tables[64] = {nullptr};
 
-TableScratch *device_tables()
+TableScratch *device_tables(int porder)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (porder < 0 || porder > MSOD_MAX_PORDER) return nullptr;
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_tables[dev]) {
         void *p = nullptr;
-        if (cudaMalloc(&p, sizeof(TableScratch)) != cudaSuccess) return nullptr;
+        if (cudaMalloc(&p, sizeof(TableScratch) * (MSOD_MAX_PORDER + 1)) != cudaSuccess) return nullptr;
         g_tables[dev] = static_cast<TableScratch *>(p);
     }
-    return g_tables[dev];
+    return g_tables[dev] + porder;
 }
 
 int *device_flags()
@@ -140,7 +143,7 @@ static int convec_impl(int porder, int nelem, int npoin, const int *connec, cons
         rc = run_check(porder, nelem, npoin, connec, (const float *)dlx, inv, ai, aj, ak, st);
         if (rc) return rc;
     }
-    TableScratch *tabs = device_tables();
+    TableScratch *tabs = device_tables(porder);
     if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
     rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
     if (rc) return rc;
@@ -172,7 +175,7 @@ static int diffu_impl(int porder, int nelem, int npoin, const int *connec, const
         rc = run_check(porder, nelem, npoin, connec, (const float *)dlx, inv, ai, aj, ak, st);
         if (rc) return rc;
     }
-    TableScratch *tabs = device_tables();
+    TableScratch *tabs = device_tables(porder);
     if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
     rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
     if (rc) return rc;
@@ -369,7 +372,7 @@ int msod_convec_ijk_mixed(int precision, int porder, int nelem, int npoin, const
         rc = run_check(porder, nelem, npoin, connec, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, st);
         if (rc) return rc;
     }
-    TableScratch *tabs = device_tables();
+    TableScratch *tabs = device_tables(porder);
     if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
     rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
     if (rc) return rc;
@@ -405,7 +408,7 @@ static int diffu_mixed_impl(int precision, int porder, int nelem, int npoin, con
         rc = run_check(porder, nelem, npoin, connec, dlx, inv, ai, aj, ak, st);
         if (rc) return rc;
     }
-    TableScratch *tabs = device_tables();
+    TableScratch *tabs = device_tables(porder);
     if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
     rc = zero_outputs(Rmass, Rmom, Rener, npoin, st);
     if (rc) return rc;

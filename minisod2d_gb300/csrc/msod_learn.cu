@@ -89,8 +89,9 @@ int prep_tables(int porder, int nelem, int npoin, const int *connec, const float
                 const float *dlxigp_ip, const int *invAtoIJK, const int *AtoI, const int *AtoJ, const int *AtoK,
                 TableScratch **out, cudaStream_t st)
 {
-    auto *tabs = static_cast<TableScratch *>(scratch(SLOT_TABLES, sizeof(TableScratch)));
-    if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
+    auto *area = static_cast<TableScratch *>(scratch(SLOT_TABLES, sizeof(TableScratch) * (MSOD_MAX_PORDER + 1)));
+    if (!area) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
+    TableScratch *tabs = area + porder;  // one table area per porder
     *out = tabs;
     ElementArgs<float> ea{};
     ea.nelem = nelem; ea.npoin = npoin; ea.connec = connec; ea.He = He; ea.gpvol = gpvol; ea.dlxigp_ip = dlxigp_ip;
@@ -98,10 +99,11 @@ int prep_tables(int porder, int nelem, int npoin, const int *connec, const float
     return cuda_rc(launch_table_prep<float>(porder, ea, tabs, st), "table preparation launch");
 }
 
-// The tables prepared by the last prep_tables call on this device.
-const TableScratch *prepared_tables()
+// The tables prepared by the last prep_tables call of this porder on this device.
+const TableScratch *prepared_tables(int porder)
 {
-    return static_cast<TableScratch *>(scratch(SLOT_TABLES, sizeof(TableScratch)));
+    return static_cast<TableScratch *>(scratch(SLOT_TABLES, sizeof(TableScratch) * (MSOD_MAX_PORDER + 1))) +
+           porder;
 }
 
 uint32_t crc32(const unsigned char *p, size_t n)
@@ -438,7 +440,7 @@ int msod_learned_viscosity(const msod_mlp *m, int porder, int nelem, int npoin, 
     a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
     a.rho = rho; a.u = u; a.p_or_T = p_or_T; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
     a.normalise = 1; a.stats = stats; a.only = fl; a.mu_e = nullptr; a.nu = nu_elem; a.numax = nullptr;
-    a.tabs = prepared_tables();  // prepared by the feature call above
+    a.tabs = prepared_tables(porder);  // prepared by the feature call above
     return cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
 }
 
@@ -473,7 +475,7 @@ int msod_diffusion_ijk_learned(const msod_mlp *m, int porder, int nelem, int npo
     a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
     a.rho = rho; a.u = u; a.p_or_T = p_or_T; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
     a.normalise = 1; a.stats = stats; a.only = fl; a.mu_e = nullptr; a.nu = nu_fb; a.numax = nullptr;
-    a.tabs = prepared_tables();  // prepared by the feature call above
+    a.tabs = prepared_tables(porder);  // prepared by the feature call above
     rc = cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
     if (rc) return rc;
     // 3. the diffusion, with the network evaluated in its prologue
