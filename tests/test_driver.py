@@ -92,3 +92,31 @@ def test_driver_run_matches_the_oracle(cuda, tmp_path):
         got = (a[:, 1], np.concatenate([a[:, 2], a[:, 3], a[:, 4]]), a[:, 5])
         for g, r64 in zip(got, ref):
             assert R.rel_l2(g, r64) < 1e-5, name
+
+
+@pytest.mark.gpu
+def test_driver_structured_mesh_matches_the_oracle(cuda, tmp_path):
+    """--mesh structured --fields smooth: the scaled shared-node workload through the driver."""
+    from minisod2d_gb300 import fem
+
+    P, nx = 2, 3
+    r = subprocess.run([_driver(), "--porder", str(P), "--mesh", "structured", "--nx", str(nx), "--jitter", "0.05",
+                        "--fields", "smooth", "--seed", "3", "--nruns", "2", "--debug", "--out", str(tmp_path)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    t = fem.element_tables(P)
+    connec, coord, nelem, npoin = fem.structured_mesh(P, nx, nx, nx, t, 0.05, 3)
+    f = fem.fields_recipe(0, 8, 3, npoin, coord)
+    n = (P + 1) ** 3
+    ot = O.element_tables(P)
+    He, gp = O.elem_jacobian(P, nelem, npoin, connec, coord, ot["dNgp"], ot["wgp"])
+    geom = dict(ot, connec=connec, He=He, gpvol=gp)
+    ones = np.ones(nelem * n, np.float32)
+    ref_c = O.full_convec_ijk(P, nelem, npoin, geom, f["u"], f["q"], f["rho"], f["pr"], f["E"], dtype=np.float64)
+    ref_d = O.full_diffusion_ijk(P, nelem, npoin, geom, 1.0, 1.0, f["rho"], f["u"], f["Tem"], f["mu_fluid"], ones,
+                                 ones, dtype=np.float64)
+    for name, ref in (("results_convec.dat", ref_c), ("results_diffu.dat", ref_d)):
+        a = np.loadtxt(tmp_path / name)
+        got = (a[:, 1], np.concatenate([a[:, 2], a[:, 3], a[:, 4]]), a[:, 5])
+        for g, r64 in zip(got, ref):
+            assert R.rel_l2(g, r64) < 2e-5, name
