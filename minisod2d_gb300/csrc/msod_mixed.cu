@@ -161,7 +161,8 @@ struct MixedGeom {
     static constexpr int NTASK = Q * Q * W;  // task: points (2w, 2w+1) of one i-row
     static constexpr int TPT = (NTASK + kThreads - 1) / kThreads;
     static constexpr int BITS = BF16 ? 8 : 11;
-    static constexpr size_t half_bytes = (size_t)2 * kNF * kPlaneB;
+    static constexpr int PB = plane_bytes<Q>();  // bytes of one field half
+    static constexpr size_t half_bytes = (size_t)2 * kNF * PB + plane_guard_bytes<Q>();
     static constexpr size_t smem = half_bytes + (size_t)(NBASE + NACC) * N * sizeof(float) +
                                    (size_t)2 * N * sizeof(int) + 2 * 32 * sizeof(float);
 };
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(kThreads)
     using G = MixedGeom<P, BF16>;
     constexpr int Q = G::Q, N = G::N, W = G::W, NTASK = G::NTASK, TPT = G::TPT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    unsigned char *sHalf = smem_raw;                                  // [2*kNF][kPlaneB]: hi, lo of each field
+    unsigned char *sHalf = smem_raw;                                  // [2*kNF][G::PB]: hi, lo of each field
     float *sBase = reinterpret_cast<float *>(sHalf + G::half_bytes);  // [NBASE][N], lattice (K*Q+J)*Q+I
     float *sAcc = sBase + NBASE * N;                                   // [NACC][N]
     int *sNode = reinterpret_cast<int *>(sAcc + NACC * N);             // [N]
@@ -297,8 +298,8 @@ __global__ void __launch_bounds__(kThreads)
             const float a = __fmul_rn(v[tk][f][0], s), b = __fmul_rn(v[tk][f][1], s);
             const float M = 12582912.0f;  // 1.5 * 2^23: adding and subtracting it rounds to an integer
             const float ha = __fsub_rn(__fadd_rn(a, M), M), hb = __fsub_rn(__fadd_rn(b, M), M);
-            *reinterpret_cast<unsigned *>(sHalf + (2 * f) * kPlaneB + off) = pack2<BF16>(ha, hb);
-            *reinterpret_cast<unsigned *>(sHalf + (2 * f + 1) * kPlaneB + off) =
+            *reinterpret_cast<unsigned *>(sHalf + (2 * f) * G::PB + off) = pack2<BF16>(ha, hb);
+            *reinterpret_cast<unsigned *>(sHalf + (2 * f + 1) * G::PB + off) =
                 pack2<BF16>(__fsub_rn(a, ha), __fsub_rn(b, hb));
         }
     }
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(kThreads)
     // operand is (hi o1, hi o2, lo o1, lo o2), row r8.
     const int m = lane >> 3, r8 = lane & 7;
     const int om = (m & 1) ? o2 : o1;
-    const int plane_off = (m >> 1) * kPlaneB;
+    const int plane_off = (m >> 1) * G::PB;
 #pragma unroll 1
     for (int d = 0; d < 3; ++d) {
         const unsigned bh = d == 0 ? Bh[0] : (d == 1 ? Bh[1] : Bh[2]);
@@ -359,9 +360,9 @@ __global__ void __launch_bounds__(kThreads)
         for (int f = 0; f < kNF; ++f) {
             unsigned a[4];
             if (d == 0)
-                ldsm_x4(a, rowp + 2 * f * kPlaneB);
+                ldsm_x4(a, rowp + 2 * f * G::PB);
             else
-                ldsm_x4_t(a, rowp + 2 * f * kPlaneB);
+                ldsm_x4_t(a, rowp + 2 * f * G::PB);
             float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             mma_acc<BF16>(c, a, bh, bh);
             mma_acc<BF16>(c, a, bl, 0u);

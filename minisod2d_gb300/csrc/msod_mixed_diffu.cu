@@ -53,7 +53,8 @@ struct MixedDiffuGeom {
     static constexpr int NTASK = Q * Q * W;  // task: points (2w, 2w+1) of one i-row
     static constexpr int TPT = (NTASK + kThreads - 1) / kThreads;
     static constexpr int BITS = BF16 ? 8 : 11;
-    static constexpr size_t half_bytes = (size_t)2 * kNFX * kPlaneB;
+    static constexpr int PB = plane_bytes<Q>();  // bytes of one field half
+    static constexpr size_t half_bytes = (size_t)2 * kNFX * PB + plane_guard_bytes<Q>();
     static constexpr size_t smem = half_bytes + (size_t)(NSB + 3 * kNG + 2) * N * sizeof(float) +
                                    (size_t)2 * N * sizeof(int) + 3 * 32 * sizeof(float);
 };
@@ -83,7 +84,7 @@ __global__ void __launch_bounds__(kThreads)
     using G = MixedDiffuGeom<P, BF16>;
     constexpr int Q = G::Q, N = G::N, W = G::W, NTASK = G::NTASK, TPT = G::TPT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    unsigned char *sHalf = smem_raw;                                  // [2*kNFX][kPlaneB]
+    unsigned char *sHalf = smem_raw;                                  // [2*kNFX][G::PB]
     float *sB = reinterpret_cast<float *>(sHalf + G::half_bytes);     // [NSB][N] lattice (K*Q+J)*Q+I
     float *sG = sB + NSB * N;                                          // [15][N] iso-derivatives; then [6][N] sums
     float *sNK = sG + 3 * kNG * N;                                     // [2][N] nu_e, kappa_e
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(kThreads)
     const bool has1 = o1 < Q, has2 = warp + 4 < Q;
     const int m = lane >> 3, r8 = lane & 7;
     const int om = (m & 1) ? o2 : o1;
-    const int plane_off = (m >> 1) * kPlaneB;
+    const int plane_off = (m >> 1) * G::PB;
     const size_t np = (size_t)npoin;
     const float twoThirds = 2.0f / 3.0f;
 
@@ -220,8 +221,8 @@ __global__ void __launch_bounds__(kThreads)
                     const float s = sScale[f];
                     unsigned hi, lo;
                     split_scaled<BF16>(__fmul_rn(v[tk][f][0], s), __fmul_rn(v[tk][f][1], s), hi, lo);
-                    *reinterpret_cast<unsigned *>(sHalf + (2 * f) * kPlaneB + off) = hi;
-                    *reinterpret_cast<unsigned *>(sHalf + (2 * f + 1) * kPlaneB + off) = lo;
+                    *reinterpret_cast<unsigned *>(sHalf + (2 * f) * G::PB + off) = hi;
+                    *reinterpret_cast<unsigned *>(sHalf + (2 * f + 1) * G::PB + off) = lo;
                 }
             }
         }
@@ -238,9 +239,9 @@ __global__ void __launch_bounds__(kThreads)
             for (int f = 0; f < kNG; ++f) {
                 unsigned a[4];
                 if (d == 0)
-                    ldsm_x4(a, rowp + 2 * f * kPlaneB);
+                    ldsm_x4(a, rowp + 2 * f * G::PB);
                 else
-                    ldsm_x4_t(a, rowp + 2 * f * kPlaneB);
+                    ldsm_x4_t(a, rowp + 2 * f * G::PB);
                 float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
                 mma_acc<BF16>(c, a, bh, bh);
                 mma_acc<BF16>(c, a, bl, 0u);
@@ -351,8 +352,8 @@ __global__ void __launch_bounds__(kThreads)
                     const float s = sScale[kNG + x];
                     unsigned hi, lo;
                     split_scaled<BF16>(__fmul_rn(fl[tk][0][x], s), __fmul_rn(fl[tk][1][x], s), hi, lo);
-                    *reinterpret_cast<unsigned *>(sHalf + (2 * x) * kPlaneB + off) = hi;
-                    *reinterpret_cast<unsigned *>(sHalf + (2 * x + 1) * kPlaneB + off) = lo;
+                    *reinterpret_cast<unsigned *>(sHalf + (2 * x) * G::PB + off) = hi;
+                    *reinterpret_cast<unsigned *>(sHalf + (2 * x + 1) * G::PB + off) = lo;
                 }
             }
         }
@@ -378,9 +379,9 @@ __global__ void __launch_bounds__(kThreads)
                 const int fx = d * kNX + x;
                 unsigned a[4];
                 if (d == 0)
-                    ldsm_x4(a, rowp + 2 * fx * kPlaneB);
+                    ldsm_x4(a, rowp + 2 * fx * G::PB);
                 else
-                    ldsm_x4_t(a, rowp + 2 * fx * kPlaneB);
+                    ldsm_x4_t(a, rowp + 2 * fx * G::PB);
                 float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
                 mma_acc<BF16>(c, a, bh, bh);
                 mma_acc<BF16>(c, a, bl, 0u);
