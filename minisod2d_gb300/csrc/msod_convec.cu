@@ -44,10 +44,6 @@
 #ifndef CONVEC_MINB5
 #define CONVEC_MINB5 3
 #endif
-// Blocks per SM for the 256-thread blocks of porder 5.
-#ifndef CONVEC_MINB_WIDE
-#define CONVEC_MINB_WIDE 1
-#endif
 
 namespace msod {
 namespace {
@@ -529,9 +525,7 @@ template <typename real, int P>
 constexpr int convec_minb()
 {
     using G = ConvecGeom<real, P>;
-    return (sizeof(real) == 4 && G::S == 1 && G::NT <= 128 && P >= 3) ? (P == 5 ? CONVEC_MINB5 : CONVEC_MINB)
-           : (sizeof(real) == 4 && G::S == 1 && P >= 3)               ? CONVEC_MINB_WIDE
-                                                                      : 1;
+    return (sizeof(real) == 4 && G::S == 1 && G::NT <= 128 && P >= 3) ? (P == 5 ? CONVEC_MINB5 : CONVEC_MINB) : 1;
 }
 
 template <typename real, int P>

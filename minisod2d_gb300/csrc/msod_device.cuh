@@ -52,9 +52,6 @@ struct LineGeom {
     static constexpr int NE = NE0 < NECAP ? NE0 : (NECAP > 0 ? NECAP : 1);
     static constexpr int NT = ((NE * TPE + 31) / 32) * 32;
     static constexpr int NPL = NE * ES;  // words per shared-memory plane
-    // Blocks per SM the register budget is sized for (__launch_bounds__):
-    // three 128-thread blocks (170 registers) for FP32 up to porder 4.
-    static constexpr int MINB = (sizeof(real) == 4 && NT <= 128) ? 3 : 1;
 };
 
 // Largest element count per block whose `planes` shared-memory planes of
