@@ -81,8 +81,11 @@ using ConvecGeom = LineGeom<real, P, (sizeof(real) == 4 && P == 5) ? CONVEC_NE5 
 // c_CDp[P][(d*Q + c)*H + m] = (D[d][2m][c], D[d][2m+1][c]), H = (Q+1)/2.
 __constant__ float2 c_CDp[MSOD_MAX_PORDER + 1][kTableDPairMax / 2];
 
-// Packed (f32x2) line passes: 0 never, 1 at porder 5, 2 whenever FP32 runs
-// one thread per line.
+// Packed (f32x2) line passes: 0 never; 1 at odd porders >= 3, where the Q
+// rows pair with no padded row (porder 3: 1.27 -> 1.23 ms on 80^3 hexes,
+// porder 5: 3.62 -> 3.05 ms on 64^3; the padded pair makes porders 2 and 4
+// slower: 1.83 -> 2.59 and 1.64 -> 2.37 ms); 2 whenever FP32 runs one thread
+// per line.
 #ifndef CONVEC_X2
 #define CONVEC_X2 1
 #endif
@@ -505,7 +508,8 @@ __device__ __forceinline__ void convec_pass_x2(const float *__restrict__ sF, flo
 template <typename real, int P>
 constexpr bool convec_packed()
 {
-    return (CONVEC_X2 == 2 || (CONVEC_X2 == 1 && P == 5)) && sizeof(real) == 4 && ConvecGeom<real, P>::S == 1;
+    return (CONVEC_X2 == 2 || (CONVEC_X2 == 1 && P % 2 == 1 && P >= 3)) && sizeof(real) == 4 &&
+           ConvecGeom<real, P>::S == 1;
 }
 
 template <typename real, int P, int DIR>
