@@ -29,12 +29,29 @@
 //   3. three line passes apply the transposed 1-D derivative matrix along the
 //      lines (the weak divergence), accumulating five sums per node through
 //      shared memory; the last pass scatter-adds with red.global.add.
+// With one thread per line from porder 3 up, the zeta derivative pass, the
+// point pass and the zeta divergence pass run as one pass over each zeta line
+// (the zeta derivatives and fluxes never reach shared memory, the He rows are
+// loaded there one point ahead), and the flux region shrinks from 18 planes to
+// 12: porder 4 then takes 53.8 KB of shared memory per block instead of 68.8 KB,
+// three blocks leave ~88 KB of L1 instead of ~28 KB for the He and node-field
+// loads, and the kernel runs 1.50 ms instead of 1.82 ms on 64^3 hexes (the same
+// fusion with the 18-plane region: 1.79 ms; four blocks per SM at 128
+// registers, which fill the shared memory again: 1.90 ms).
 // The 1-D derivative matrices are constant-bank operands.
 #include <cuda_runtime.h>
 
 #include "msod_device.cuh"
 #include "msod_kernels.h"
 #include "msod_mlp.cuh"
+
+// Zeta stage (one thread per line only): 1 = the zeta derivatives, the point
+// pass and the zeta divergence run as one pass over each zeta line, with the
+// zeta derivatives and fluxes in registers; 0 = three line passes, a point
+// pass over all points, three divergence passes.
+#ifndef DIFFU_FUSEZ
+#define DIFFU_FUSEZ 1
+#endif
 
 // Lattices of gathered node fields: 2 = double-buffered (the next group's
 // fields are gathered with cp.async while the current group is computed),
@@ -104,7 +121,7 @@ __device__ __forceinline__ void grad_pass(const LineThread<G> &lt, const typenam
 
 // Pass 2, direction DIR: weak divergence along the lines with the transposed
 // derivative matrix; partial sums through planes P_DR.. of the stage.
-template <class G, int DIR>
+template <class G, int DIR, bool FIRST, bool LAST>
 __device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::real *__restrict__ sF,
                                          const typename G::real *__restrict__ sX, const typename G::real *__restrict__ sD,
                                          const int *__restrict__ sNode, int npoin,
@@ -127,7 +144,7 @@ __device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::re
         const int o = base + lt.rc(rr) * OST;
         kap[rr] = sF[P_KAP * NPL + o];
 #pragma unroll
-        for (int k = 0; k < 5; ++k) acc[rr][k] = DIR == 0 ? (real)0 : sF[(P_DR + k) * NPL + o];
+        for (int k = 0; k < 5; ++k) acc[rr][k] = FIRST ? (real)0 : sF[(P_DR + k) * NPL + o];
     }
 #pragma unroll
     for (int x = 0; x < NX; ++x) {
@@ -150,7 +167,7 @@ __device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::re
     for (int rr = 0; rr < R; ++rr) {
         if (!lt.owns(rr)) continue;
         const int o = base + (lt.r0 + rr) * OST;
-        if (DIR < 2) {
+        if (!LAST) {
 #pragma unroll
             for (int k = 0; k < 5; ++k) sF[(P_DR + k) * NPL + o] = acc[rr][k];
         } else {
@@ -164,10 +181,78 @@ __device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::re
     }
 }
 
+// Point pass at one point: physical gradients of rho, T, u from the
+// iso-parametric ones gi[d][f] (He(ii, j) = H[j*3 + ii]), the stress and
+// tau u, and the contravariant fluxes F[d][x] = gpvol He(:,d)^T X_x.
+template <typename real>
+__device__ __forceinline__ void point_flux(const real (&gi)[3][5], real r, const real (&uu)[3], real muf, real ms,
+                                           real me, const real (&H)[9], real gv, real (&F)[3][NX])
+{
+    const real twoThirds = (real)2 / (real)3;
+    real gR[3], gT[3], gU[3][3];
+#pragma unroll
+    for (int ii = 0; ii < 3; ++ii) {
+        gR[ii] = H[ii] * gi[0][D_RHO] + H[3 + ii] * gi[1][D_RHO] + H[6 + ii] * gi[2][D_RHO];
+        gT[ii] = H[ii] * gi[0][D_T] + H[3 + ii] * gi[1][D_T] + H[6 + ii] * gi[2][D_T];
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            gU[ii][j] = H[j] * gi[0][D_U0 + ii] + H[3 + j] * gi[1][D_U0 + ii] + H[6 + j] * gi[2][D_U0 + ii];
+    }
+    const real mu_fgp = muf + r * ms;
+    const real mu_tot = mu_fgp + me;
+    const real divU = gU[0][0] + gU[1][1] + gU[2][2];
+    real tau[3][3], tauU[3];
+#pragma unroll
+    for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tau[ii][j] = mu_tot * (gU[ii][j] + gU[j][ii]);
+#pragma unroll
+    for (int ii = 0; ii < 3; ++ii) tau[ii][ii] -= mu_fgp * twoThirds * divU;
+#pragma unroll
+    for (int ii = 0; ii < 3; ++ii) tauU[ii] = tau[ii][0] * uu[0] + tau[ii][1] * uu[1] + tau[ii][2] * uu[2];
+    const real *Xv[NX] = {gR, tauU, gT, tau[0], tau[1], tau[2]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int x = 0; x < NX; ++x)
+            F[d][x] = gv * (H[d * 3] * Xv[x][0] + H[d * 3 + 1] * Xv[x][1] + H[d * 3 + 2] * Xv[x][2]);
+}
+
+// The fused zeta stage runs where one thread owns a line, from porder 3 up
+// (porder 2 on 120^3 hexes: 1.98 ms unfused, 2.03 ms fused).
+template <class G>
+constexpr bool diffu_fusez()
+{
+    return DIFFU_FUSEZ != 0 && G::S == 1 && G::P >= 3;
+}
+// Flux planes: three directions, or two with the fused zeta stage (the zeta
+// derivatives and fluxes stay in registers).
+template <class G>
+constexpr int diffu_xplanes()
+{
+    return (diffu_fusez<G>() ? 2 : 3) * NX;
+}
+
+// He rows of the fused zeta stage: 0 = the line's rows in registers from the
+// start of the group (across the gradient passes), 1 = each point's row loaded
+// in the stage one point ahead (fewer registers).
+#ifndef DIFFU_HE_LATE
+#define DIFFU_HE_LATE 1
+#endif
+// Blocks per SM the FP32 porder-4 kernel is compiled for (register cap).
+#ifndef DIFFU_MINB4
+#define DIFFU_MINB4 1
+#endif
+template <class G>
+constexpr int diffu_minb()
+{
+    return (sizeof(typename G::real) == 4 && G::P == 4) ? DIFFU_MINB4 : 1;
+}
+
 template <class G>
 constexpr size_t diffu_smem_bytes()
 {
-    return (size_t)(DIFFU_NBUF * NDF + 3 * NX) * G::NPL * sizeof(typename G::real) +
+    return (size_t)(DIFFU_NBUF * NDF + diffu_xplanes<G>()) * G::NPL * sizeof(typename G::real) +
            (size_t)3 * G::Q * G::Q * sizeof(typename G::real) +
            (size_t)(DIFFU_NBUF * G::NPL + 2 * G::N) * sizeof(int);
 }
@@ -188,9 +273,20 @@ constexpr int diffu_s()
     return sizeof(real) == 4 ? (P == 4 ? DIFFU_S4 : (P == 5 ? DIFFU_S5 : 0)) : 0;
 }
 
+// Elements per block of the FP32 porder-4 diffusion (0: the default, five).
+#ifndef DIFFU_NE4
+#define DIFFU_NE4 0
+#endif
 template <typename real, int P>
-using DiffuGeom = LineGeom<real, P, necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES, (int)sizeof(real), 200 * 1024),
-                           diffu_s<real, P>()>;
+constexpr int diffu_necap()
+{
+    return (sizeof(real) == 4 && P == 4 && DIFFU_NE4 > 0)
+               ? DIFFU_NE4
+               : necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES, (int)sizeof(real), 200 * 1024);
+}
+
+template <typename real, int P>
+using DiffuGeom = LineGeom<real, P, diffu_necap<real, P>(), diffu_s<real, P>()>;
 
 // Viscosity source of the diffusion kernel.
 enum { VISC_MU_E = 0, VISC_NU_ELEM = 1, VISC_NET = 2 };
@@ -209,7 +305,7 @@ constexpr size_t net_smem_floats()
 }
 
 template <class G, int VISC>
-__global__ void __launch_bounds__(G::NT)
+__global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     diffu_kernel(int nelem, int npoin, int ngroups, const int *__restrict__ connec,
                  const typename G::real *__restrict__ He, const typename G::real *__restrict__ gpvol,
                  const TableScratch *__restrict__ tabs, typename G::real Cp, typename G::real Pr,
@@ -225,8 +321,8 @@ __global__ void __launch_bounds__(G::NT)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NBUF = DIFFU_NBUF;
     real *sF = reinterpret_cast<real *>(smem_raw);  // [NBUF][NDF][NPL]
-    real *sX = sF + NBUF * NDF * NPL;                // [3*NX][NPL]
-    real *sD = sX + 3 * NX * NPL;                    // [3][Q][Q] (several threads per line)
+    real *sX = sF + NBUF * NDF * NPL;                // [2 or 3 NX][NPL]
+    real *sD = sX + diffu_xplanes<G>() * NPL;        // [3][Q][Q] (several threads per line)
     int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);  // [NBUF][NPL]
     int *sPerm = sNode + NBUF * NPL;
     int *sLat = sPerm + N;
@@ -235,6 +331,10 @@ __global__ void __launch_bounds__(G::NT)
     float *sInfo = sFeat + NE * kMlpIn;                   // [NE][4]: numax, flag, fallback nu, nu
 
     const int tid = threadIdx.x;
+    const LineThread<G> lt(tid);
+    constexpr bool FUSEZ = diffu_fusez<G>();
+    constexpr bool LATE = FUSEZ && DIFFU_HE_LATE != 0;
+    constexpr int MP = LATE ? 1 : (FUSEZ ? Q : IPT);  // points whose He and gpvol a thread holds
     for (int i = tid; i < N; i += NT) {
         sPerm[i] = tabs->perm[i];
         sLat[i] = tabs->lat[i];
@@ -381,13 +481,15 @@ __global__ void __launch_bounds__(G::NT)
         }
         cp_async_commit();
     };
-    // He(:,:) and gpvol of the thread's point-pass points (lattice order).
-    auto load_metric = [&](int g, real (&Hm)[IPT][9], real (&gv)[IPT]) {
+    // He(:,:) and gpvol of the thread's point-pass points: items tid + k NT
+    // (lattice order), or the points of its zeta line in the zeta stage.
+    auto load_metric = [&](int g, real (&Hm)[MP][9], real (&gv)[MP]) {
 #pragma unroll
-        for (int k = 0; k < IPT; ++k) {
+        for (int k = 0; k < MP; ++k) {
             const int i = tid + k * NT;
-            const int el = i / N, l = i - el * N, e = g * NE + el;
-            const bool ok = i < NE * N && e < nelem;
+            const int el = FUSEZ ? lt.el : i / N;
+            const int l = FUSEZ ? line_lat<2, Q>(lt.la, lt.lb, k) : i - el * N, e = g * NE + el;
+            const bool ok = (FUSEZ ? lt.active : i < NE * N) && e < nelem;
             const int a = ok ? sPerm[l] : 0;
             const real *hp = He + (ok ? ((size_t)e * N + a) * 9 : 0);
 #pragma unroll
@@ -408,14 +510,12 @@ __global__ void __launch_bounds__(G::NT)
     int gn = g + stride;
     if (gn < ngroups) load_ids(gn, ids);
 
-    const LineThread<G> lt(tid);
-    const real twoThirds = (real)2 / (real)3;
     int s = 0;
     for (; g < ngroups; g = gn, gn += stride, s = NBUF == 2 ? s ^ 1 : 0) {
         real *sFs = sF + s * NDF * NPL;
         int *sNs = sNode + s * NPL;
-        real Hm[IPT][9], gv[IPT];
-        load_metric(g, Hm, gv);
+        real Hm[MP][9], gv[MP];
+        if (!LATE) load_metric(g, Hm, gv);
         if (NBUF == 2 && gn < ngroups) store_ids(ids, sNode + (s ^ 1) * NPL);
         store_net();
         cp_async_wait_all();
@@ -428,70 +528,151 @@ __global__ void __launch_bounds__(G::NT)
             load_net(gn);
         }
         run_net(g);
-        if (lt.active) {
-            grad_pass<G, 0>(lt, sFs, sX, sD);
-            grad_pass<G, 1>(lt, sFs, sX, sD);
-            grad_pass<G, 2>(lt, sFs, sX, sD);
-        }
-        __syncthreads();
-        // Point pass: physical gradients, stress and contravariant fluxes.
-#pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            const int i = tid + k * NT;
-            if (i >= NE * N) break;
-            const int el = i / N, l = i - el * N;
-            const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
-            real gi[3][5];
-#pragma unroll
-            for (int d = 0; d < 3; ++d)
-#pragma unroll
-                for (int f = 0; f < 5; ++f) gi[d][f] = sX[(d * 5 + f) * NPL + o];
-            const real r = sFs[D_RHO * NPL + o];
-            const real uu[3] = {sFs[D_U0 * NPL + o], sFs[D_U1 * NPL + o], sFs[D_U2 * NPL + o]};
-            const int ee = g * NE + el;
-            const real muf = sFs[D_MUF * NPL + o], ms = sFs[D_MUS * NPL + o];
-            const real me = VISC == VISC_NU_ELEM ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0)
-                            : VISC == VISC_NET  ? r * (real)sInfo[el * 4 + 3]
-                                                : sFs[D_MUE * NPL + o];
-            // Hm[k][j*3+ii] = He(ii, j)
-            real gR[3], gT[3], gU[3][3];
-#pragma unroll
-            for (int ii = 0; ii < 3; ++ii) {
-                gR[ii] = Hm[k][ii] * gi[0][D_RHO] + Hm[k][3 + ii] * gi[1][D_RHO] + Hm[k][6 + ii] * gi[2][D_RHO];
-                gT[ii] = Hm[k][ii] * gi[0][D_T] + Hm[k][3 + ii] * gi[1][D_T] + Hm[k][6 + ii] * gi[2][D_T];
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-                    gU[ii][j] = Hm[k][j] * gi[0][D_U0 + ii] + Hm[k][3 + j] * gi[1][D_U0 + ii] +
-                                Hm[k][6 + j] * gi[2][D_U0 + ii];
+        if constexpr (FUSEZ) {
+            if (lt.active) {
+                grad_pass<G, 0>(lt, sFs, sX, sD);
+                grad_pass<G, 1>(lt, sFs, sX, sD);
             }
-            const real mu_fgp = muf + r * ms;
-            const real mu_tot = mu_fgp + me;
-            const real divU = gU[0][0] + gU[1][1] + gU[2][2];
-            real tau[3][3], tauU[3];
+            __syncthreads();
+            // Zeta stage, one thread per zeta line: the zeta derivatives at the
+            // line's points (from its nodal values in registers), the point
+            // pass there (the xi and eta fluxes are stored for their
+            // divergence passes) and the zeta divergence of the zeta fluxes,
+            // which stay in registers; the partial sums start the divergence.
+            if (lt.active) {
+                constexpr int OST = Q * QP;
+                const int base = lt.el * ES + line_off<2, Q, QP>(lt.la, lt.lb, 0);
+                real v[5][Q];
 #pragma unroll
-            for (int ii = 0; ii < 3; ++ii)
+                for (int f = 0; f < 5; ++f)
 #pragma unroll
-                for (int j = 0; j < 3; ++j) tau[ii][j] = mu_tot * (gU[ii][j] + gU[j][ii]);
+                    for (int c = 0; c < Q; ++c) v[f][c] = sFs[f * NPL + base + c * OST];
+                real acc[Q][5], accT[Q], kap[Q];
 #pragma unroll
-            for (int ii = 0; ii < 3; ++ii) tau[ii][ii] -= mu_fgp * twoThirds * divU;
+                for (int rr = 0; rr < Q; ++rr) {
+                    accT[rr] = (real)0;
 #pragma unroll
-            for (int ii = 0; ii < 3; ++ii) tauU[ii] = tau[ii][0] * uu[0] + tau[ii][1] * uu[1] + tau[ii][2] * uu[2];
-            const real *Xv[NX] = {gR, tauU, gT, tau[0], tau[1], tau[2]};
+                    for (int k = 0; k < 5; ++k) acc[rr][k] = (real)0;
+                }
+                const int ee = g * NE + lt.el;
+                const bool eok = ee < nelem;
+                // Late He rows: point c's row and gpvol, issued one point ahead.
+                auto he_row = [&](int c, real (&h)[9], real &gp) {
+                    const int a = sPerm[line_lat<2, Q>(lt.la, lt.lb, c)];
+                    const real *hp = He + (eok ? ((size_t)ee * N + a) * 9 : 0);
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
+                    for (int j = 0; j < 9; ++j) h[j] = eok ? ldg(hp + j) : (real)0;
+                    gp = eok ? ldg(gpvol + (size_t)ee * N + a) : (real)0;
+                };
+                real Hn[9], gpn;
+                if constexpr (LATE) he_row(0, Hn, gpn);
 #pragma unroll
-                for (int x = 0; x < NX; ++x)
-                    sX[(d * NX + x) * NPL + o] =
-                        gv[k] * (Hm[k][d * 3] * Xv[x][0] + Hm[k][d * 3 + 1] * Xv[x][1] + Hm[k][d * 3 + 2] * Xv[x][2]);
-            sFs[P_NUE * NPL + o] = me / r;
-            sFs[P_KAP * NPL + o] = muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
+                for (int c = 0; c < Q; ++c) {
+                    const int o = base + c * OST;
+                    real Hc[9], gc;
+                    if constexpr (LATE) {
+#pragma unroll
+                        for (int j = 0; j < 9; ++j) Hc[j] = Hn[j];
+                        gc = gpn;
+                        if (c + 1 < Q) he_row(c + 1, Hn, gpn);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 9; ++j) Hc[j] = Hm[c][j];
+                        gc = gv[c];
+                    }
+                    real gi[3][5];
+#pragma unroll
+                    for (int d = 0; d < 2; ++d)
+#pragma unroll
+                        for (int f = 0; f < 5; ++f) gi[d][f] = sX[(d * 5 + f) * NPL + o];
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) {
+                        real t = (real)0;
+#pragma unroll
+                        for (int j = 0; j < Q; ++j) t = fma(cD<real>(G::P, (2 * Q + c) * Q + j), v[f][j], t);
+                        gi[2][f] = t;
+                    }
+                    const real r = v[D_RHO][c];
+                    const real uu[3] = {v[D_U0][c], v[D_U1][c], v[D_U2][c]};
+                    const real muf = sFs[D_MUF * NPL + o], ms = sFs[D_MUS * NPL + o];
+                    const real me = VISC == VISC_NU_ELEM ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0)
+                                    : VISC == VISC_NET  ? r * (real)sInfo[lt.el * 4 + 3]
+                                                        : sFs[D_MUE * NPL + o];
+                    real F[3][NX];
+                    point_flux(gi, r, uu, muf, ms, me, Hc, gc, F);
+#pragma unroll
+                    for (int d = 0; d < 2; ++d)
+#pragma unroll
+                        for (int x = 0; x < NX; ++x) sX[(d * NX + x) * NPL + o] = F[d][x];
+#pragma unroll
+                    for (int rr = 0; rr < Q; ++rr) {
+                        const real w = cD<real>(G::P, (2 * Q + c) * Q + rr);
+                        acc[rr][0] = fma(w, F[2][X_GRHO], acc[rr][0]);
+                        acc[rr][1] = fma(w, F[2][X_TAUU], acc[rr][1]);
+                        accT[rr] = fma(w, F[2][X_GT], accT[rr]);
+#pragma unroll
+                        for (int m = 0; m < 3; ++m) acc[rr][2 + m] = fma(w, F[2][X_TAU0 + m], acc[rr][2 + m]);
+                    }
+                    // rho and T of this point are in registers or no longer
+                    // needed: their planes take nu_e and kappa_e.
+                    kap[c] = muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
+                    sFs[P_NUE * NPL + o] = me / r;
+                    sFs[P_KAP * NPL + o] = kap[c];
+                }
+#pragma unroll
+                for (int rr = 0; rr < Q; ++rr) {
+                    const int o = base + rr * OST;
+                    acc[rr][1] = fma(kap[rr], accT[rr], acc[rr][1]);
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) sFs[(P_DR + k) * NPL + o] = acc[rr][k];
+                }
+            }
+            __syncthreads();
+            if (lt.active) div_pass<G, 0, false, false>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            __syncthreads();
+            if (lt.active) div_pass<G, 1, false, true>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+        } else {
+            if (lt.active) {
+                grad_pass<G, 0>(lt, sFs, sX, sD);
+                grad_pass<G, 1>(lt, sFs, sX, sD);
+                grad_pass<G, 2>(lt, sFs, sX, sD);
+            }
+            __syncthreads();
+            // Point pass: physical gradients, stress and contravariant fluxes.
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const int i = tid + k * NT;
+                if (i >= NE * N) break;
+                const int el = i / N, l = i - el * N;
+                const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
+                real gi[3][5];
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) gi[d][f] = sX[(d * 5 + f) * NPL + o];
+                const real r = sFs[D_RHO * NPL + o];
+                const real uu[3] = {sFs[D_U0 * NPL + o], sFs[D_U1 * NPL + o], sFs[D_U2 * NPL + o]};
+                const int ee = g * NE + el;
+                const real muf = sFs[D_MUF * NPL + o], ms = sFs[D_MUS * NPL + o];
+                const real me = VISC == VISC_NU_ELEM ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0)
+                                : VISC == VISC_NET  ? r * (real)sInfo[el * 4 + 3]
+                                                    : sFs[D_MUE * NPL + o];
+                real F[3][NX];
+                point_flux(gi, r, uu, muf, ms, me, Hm[k], gv[k], F);
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+#pragma unroll
+                    for (int x = 0; x < NX; ++x) sX[(d * NX + x) * NPL + o] = F[d][x];
+                sFs[P_NUE * NPL + o] = me / r;
+                sFs[P_KAP * NPL + o] = muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
+            }
+            __syncthreads();
+            if (lt.active) div_pass<G, 0, true, false>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            __syncthreads();
+            if (lt.active) div_pass<G, 1, false, false>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            __syncthreads();
+            if (lt.active) div_pass<G, 2, false, true>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
         }
-        __syncthreads();
-        if (lt.active) div_pass<G, 0>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
-        __syncthreads();
-        if (lt.active) div_pass<G, 1>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
-        __syncthreads();
-        if (lt.active) div_pass<G, 2>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
         __syncthreads();
         if (NBUF == 1 && gn < ngroups) {  // the next group's node ids, then its fields
             store_ids(ids, sNode);
