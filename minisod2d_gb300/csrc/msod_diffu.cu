@@ -259,13 +259,15 @@ constexpr size_t diffu_smem_bytes()
 
 // Threads per line of the FP32 diffusion (0: the line-geometry default, one).
 // Measured on 64^3 hexes: porder 4 is fastest with one (1.84 ms; 2.08-2.27 ms
-// with 2, 3 or 5: more warps, but the line loads are repeated per thread),
-// porder 5 with two (3.79 ms against 3.99 ms with one).
+// with 2, 3 or 5: more warps, but the line loads are repeated per thread).
+// Porder 5 with one and the fused zeta stage, three elements per 128-thread
+// block: 2.97 ms, against 3.78 ms with two threads per line (three elements per
+// 224-thread block, unfused) and 3.19 ms with one at two elements per block.
 #ifndef DIFFU_S4
 #define DIFFU_S4 0
 #endif
 #ifndef DIFFU_S5
-#define DIFFU_S5 2
+#define DIFFU_S5 1
 #endif
 template <typename real, int P>
 constexpr int diffu_s()
@@ -273,16 +275,21 @@ constexpr int diffu_s()
     return sizeof(real) == 4 ? (P == 4 ? DIFFU_S4 : (P == 5 ? DIFFU_S5 : 0)) : 0;
 }
 
-// Elements per block of the FP32 porder-4 diffusion (0: the default, five).
+// Elements per block of the FP32 porder-4 / porder-5 diffusion (0: the
+// line-geometry default).
 #ifndef DIFFU_NE4
 #define DIFFU_NE4 0
+#endif
+#ifndef DIFFU_NE5
+#define DIFFU_NE5 3
 #endif
 template <typename real, int P>
 constexpr int diffu_necap()
 {
-    return (sizeof(real) == 4 && P == 4 && DIFFU_NE4 > 0)
-               ? DIFFU_NE4
-               : necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES, (int)sizeof(real), 200 * 1024);
+    return (sizeof(real) == 4 && P == 4 && DIFFU_NE4 > 0)   ? DIFFU_NE4
+           : (sizeof(real) == 4 && P == 5 && DIFFU_NE5 > 0) ? DIFFU_NE5
+                                                             : necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES,
+                                                                         (int)sizeof(real), 200 * 1024);
 }
 
 template <typename real, int P>
