@@ -325,6 +325,15 @@ __global__ void __launch_bounds__(G::NT)
 template <int P>
 using ViscGeom = LineGeom<float, P>;
 
+// Preferred shared-memory carveout of the porder-5 estimator, percent of the
+// maximum (-1: none). Its 51.5 KB blocks fill a 228 KB carveout four to an SM
+// and leave ~28 KB of L1; at 58 % (132 KB: two blocks, ~124 KB of L1) it runs
+// 1.80 ms instead of 2.36 ms on 64^3 hexes (72 %, three blocks: 1.86 ms).
+// Porder 4 measures the same with or without (0.89 ms).
+#ifndef VISC_CARVE5
+#define VISC_CARVE5 58
+#endif
+
 template <int P>
 cudaError_t visc_p(const ViscArgs &a, cudaStream_t st)
 {
@@ -336,6 +345,10 @@ cudaError_t visc_p(const ViscArgs &a, cudaStream_t st)
     if (!a.tabs) return cudaErrorInvalidValue;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
+    if (P == 5 && VISC_CARVE5 >= 0) {
+        err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, VISC_CARVE5);
+        if (err != cudaSuccess) return err;
+    }
     if (G::S == 1) {
         err = cudaMemcpyToSymbolAsync(c_VD, a.tabs->Df, sizeof(float) * 3 * G::Q * G::Q, sizeof(float) * kTableDMax * P,
                                       cudaMemcpyDeviceToDevice, st);
