@@ -63,7 +63,7 @@ extern "C" {
 #define MSOD_ERR_BAD_TABLES 4   /* element tables or connectivity failed validation   */
 #define MSOD_ERR_NO_DEVICE 5    /* no usable CUDA device                              */
 #define MSOD_ERR_INTERNAL 6
-#define MSOD_ERR_UNSUPPORTED 7  /* a mode or option this build does not provide       */
+#define MSOD_ERR_UNSUPPORTED 7  /* a mode or option the library was not compiled with */
 #define MSOD_ERR_BAD_MODEL 8    /* a network weight file is malformed or fails its CRC */
 
 /* Per-element learned viscosity: 12 features -> 32 -> 32 -> 1 parameters. */
