@@ -239,14 +239,28 @@ constexpr int diffu_xplanes()
 #ifndef DIFFU_HE_LATE
 #define DIFFU_HE_LATE 1
 #endif
-// Blocks per SM the FP32 porder-4 kernel is compiled for (register cap).
+// Minimum blocks per SM in the launch bounds. The kernels with the fused zeta
+// stage take 1, which lets the compiler spend registers (porder 4: 137 / 153 /
+// 153 for the three viscosity sources, porder 5: 159-163); this holds them to
+// three blocks per SM and keeps the L1 that the larger carveout of a fourth
+// block would take (DIFFU_MINB4 = 4, 128 registers: 1.90 ms against 1.50 ms,
+// porder 4 on 64^3). The other kernels take 0, the block-size-only heuristic
+// (a 1 there raised porder 6 from 115 to 154 registers: one block per SM
+// instead of two).
 #ifndef DIFFU_MINB4
 #define DIFFU_MINB4 1
 #endif
 template <class G>
 constexpr int diffu_minb()
 {
-    return (sizeof(typename G::real) == 4 && G::P == 4) ? DIFFU_MINB4 : 1;
+    return diffu_fusez<G>() ? ((sizeof(typename G::real) == 4 && G::P == 4) ? DIFFU_MINB4 : 1) : 0;
+}
+
+// kappa_e at a node (elem_diffu.f90:143-146).
+template <typename real>
+__device__ __forceinline__ real kappa_e(real muf, real me, real ms, real r, real Cp, real Pr)
+{
+    return muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
 }
 
 template <class G>
@@ -505,6 +519,14 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
         }
     };
 
+    // mu_e at a point of element el of group g (lattice offset o, density r).
+    auto point_mu_e = [&](int g, int el, int o, real r, const real *sFs) -> real {
+        const int ee = g * NE + el;
+        return VISC == VISC_NU_ELEM ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0)
+               : VISC == VISC_NET  ? r * (real)sInfo[el * 4 + 3]
+                                   : sFs[D_MUE * NPL + o];
+    };
+
     int g = blockIdx.x;
     const int stride = gridDim.x;
     int ids[IPT];
@@ -602,9 +624,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                     const real r = v[D_RHO][c];
                     const real uu[3] = {v[D_U0][c], v[D_U1][c], v[D_U2][c]};
                     const real muf = sFs[D_MUF * NPL + o], ms = sFs[D_MUS * NPL + o];
-                    const real me = VISC == VISC_NU_ELEM ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0)
-                                    : VISC == VISC_NET  ? r * (real)sInfo[lt.el * 4 + 3]
-                                                        : sFs[D_MUE * NPL + o];
+                    const real me = point_mu_e(g, lt.el, o, r, sFs);
                     real F[3][NX];
                     point_flux(gi, r, uu, muf, ms, me, Hc, gc, F);
 #pragma unroll
@@ -622,7 +642,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                     }
                     // rho and T of this point are in registers or no longer
                     // needed: their planes take nu_e and kappa_e.
-                    kap[c] = muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
+                    kap[c] = kappa_e(muf, me, ms, r, Cp, Pr);
                     sFs[P_NUE * NPL + o] = me / r;
                     sFs[P_KAP * NPL + o] = kap[c];
                 }
@@ -659,11 +679,8 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                     for (int f = 0; f < 5; ++f) gi[d][f] = sX[(d * 5 + f) * NPL + o];
                 const real r = sFs[D_RHO * NPL + o];
                 const real uu[3] = {sFs[D_U0 * NPL + o], sFs[D_U1 * NPL + o], sFs[D_U2 * NPL + o]};
-                const int ee = g * NE + el;
                 const real muf = sFs[D_MUF * NPL + o], ms = sFs[D_MUS * NPL + o];
-                const real me = VISC == VISC_NU_ELEM ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0)
-                                : VISC == VISC_NET  ? r * (real)sInfo[el * 4 + 3]
-                                                    : sFs[D_MUE * NPL + o];
+                const real me = point_mu_e(g, el, o, r, sFs);
                 real F[3][NX];
                 point_flux(gi, r, uu, muf, ms, me, Hm[k], gv[k], F);
 #pragma unroll
@@ -671,7 +688,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
 #pragma unroll
                     for (int x = 0; x < NX; ++x) sX[(d * NX + x) * NPL + o] = F[d][x];
                 sFs[P_NUE * NPL + o] = me / r;
-                sFs[P_KAP * NPL + o] = muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
+                sFs[P_KAP * NPL + o] = kappa_e(muf, me, ms, r, Cp, Pr);
             }
             __syncthreads();
             if (lt.active) div_pass<G, 0, true, false>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
