@@ -215,13 +215,34 @@ def cpu_baseline(cfg, host, seconds=15.0):
                       "prorated by element share" % (ne, host.nelem, dt)}
 
 
+def workload_config(cfg, nelem, npoin):
+    """The `config` of both arms' JSON lines: the workload alone (arm details sit outside it)."""
+    Bc, Bd = algorithmic_bytes(nelem, cfg.nnode, npoin)
+    return {"workload": cfg.name, "porder": cfg.porder, "nelem": nelem, "npoin": npoin, "jitter": cfg.jitter,
+            "l2": "inputs %.2f GB per call > 129 MB L2, no flush" % ((Bc + Bd) / 2e9)}
+
+
+class OracleHostCase:
+    """The workload's host arrays built by the oracle alone -- element tables, structured mesh,
+    seeded fields, bit for bit those of the library's setup (tests/test_oracle_kat.py) -- so that
+    the reference arm loads no product code."""
+
+    def __init__(self, cfg):
+        from oracle import oracle as O
+
+        self.cfg = cfg
+        self.tables = O.element_tables(cfg.porder)
+        self.connec, self.coord, self.nelem, self.npoin = O.structured_mesh(cfg.porder, cfg.nx, self.tables,
+                                                                            cfg.jitter, cfg.seed)
+        self.fields = O.fields_recipe(cfg.kind, cfg.nmodes, cfg.seed, self.npoin, self.coord)
+
+
 def run_reference(args, cfg):
     """--impl reference: the reference algorithm (the oracle port) on all host cores."""
-    from minisod2d_gb300 import workload
     from oracle import oracle as O
 
     O.lib()
-    host = workload.HostCase(cfg)
+    host = OracleHostCase(cfg)
     nth = O.cpu_count()
     per_step = max(1.0, min(5.0, 90.0 / max(1, args.steps + args.warmup)))
     ns = calibrate_sample(cfg, host, nth, per_step)
@@ -238,9 +259,10 @@ def run_reference(args, cfg):
               "prorated by element share" % (ne, host.nelem, nth))
     out = {"metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-           "config": {"workload": cfg.name, "porder": cfg.porder, "nelem": host.nelem, "npoin": host.npoin,
-                      "parallelism": "host cores"},
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered structured mesh, Fourier fields)",
+           "impl": "reference", "config": workload_config(cfg, host.nelem, host.npoin),
+           "parallelism": "OpenMP element loop on %d host threads (rank 0 only)" % nth,
+           "inputs": "built by the oracle (oracle/): no product library loaded",
            "cpu_baseline": {"value": value, "unit": "GDOF/s", "cores": nth, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": "GDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -386,9 +408,8 @@ def run_ours(args, cfg, rank, local, world):
         "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered structured mesh, Fourier fields)",
-        "config": {"workload": cfg.name, "porder": cfg.porder, "nelem": dev.nelem, "npoin": dev.npoin,
-                   "jitter": cfg.jitter, "parallelism": "replica per GPU" if world > 1 else "single GPU",
-                   "l2": "inputs %.2f GB per call > 129 MB L2, no flush" % ((Bc + Bd) / 2e9)},
+        "config": workload_config(cfg, dev.nelem, dev.npoin),
+        "parallelism": "replica per GPU" if world > 1 else "single GPU",
         "roofline": {"bound": "hbm", "kernel": dom + " call (output zeroing + kernel)", "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes": dom_b},
@@ -631,9 +652,6 @@ def main():
     rank, local, world = dist_setup()
     if args.impl == "reference":
         if rank == 0:
-            from minisod2d_gb300 import build
-
-            build.build()
             run_reference(args, cfg)
         return
     run_ours(args, cfg, rank, local, world)

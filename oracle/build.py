@@ -27,7 +27,8 @@ def build(force=False, verbose=False):
     procs = []
     for real, sfx in (("float", "_f32"), ("double", "_f64")):
         obj = os.path.join(bdir, "msod_oracle%s.o" % sfx)
-        cmd = ["gcc", *CFLAGS, "-DORC_REAL=%s" % real, "-DORC_SFX=%s" % sfx, "-c", SRC, "-o", obj]
+        cmd = ["gcc", *CFLAGS, "-DORC_REAL=%s" % real, "-DORC_SFX=%s" % sfx,
+               "-DORC_IS_FLOAT=%d" % (real == "float"), "-c", SRC, "-o", obj]
         if verbose:
             print(" ".join(cmd))
         procs.append(subprocess.Popen(cmd))

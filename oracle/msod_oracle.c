@@ -48,6 +48,10 @@
 
 typedef ORC_REAL real;
 
+#ifndef ORC_IS_FLOAT
+#define ORC_IS_FLOAT 0
+#endif
+
 #define ORC_CAT2(a, b) a##b
 #define ORC_CAT(a, b) ORC_CAT2(a, b)
 #define F(name) ORC_CAT(name, ORC_SFX)
@@ -1359,3 +1363,171 @@ int F(orc_fem_diffu)(int nelem, int npoin, const int *connec, const real *Ngp, c
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Workload recipes: the structured shared-node mesh and the seeded node      */
+/* fields of the benchmark configurations (no reference counterpart: the     */
+/* reference meshes disconnected copies of one element, mod_mesh.f90:11-65,  */
+/* and sets its own initial condition, main.f90:320-361).  Restated here so   */
+/* that the CPU legs of the benchmark build their inputs without the product */
+/* library; tests/test_oracle_kat.py checks them bit for bit against it.     */
+/* FP32 build only (coordinates and fields are FP32).                        */
+/* ------------------------------------------------------------------------- */
+#if ORC_IS_FLOAT
+/* splitmix64 -> uniform doubles in [0,1) -> Box-Muller normals. */
+typedef struct { uint64_t s; } orc_rng;
+static uint64_t rng_next(orc_rng *r)
+{
+    uint64_t z = (r->s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double rng_uniform(orc_rng *r) { return (double)(rng_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+static double rng_normal(orc_rng *r)
+{
+    double u1 = rng_uniform(r), u2 = rng_uniform(r);
+    if (u1 < 1e-300) u1 = 1e-300;
+    return sqrt(-2.0 * log(u1)) * cos(2.0 * M_PI * u2);
+}
+typedef struct { double k[3], phase, amp[3]; } orc_mode;
+/* nmodes Fourier modes: integer wavevectors in [-kmax,kmax]^3 (not all zero),
+ * uniform phases, per-component N(0, amp_sigma) amplitudes. */
+static void make_modes(orc_rng *r, int nmodes, int kmax, double amp_sigma, orc_mode *m)
+{
+    for (int i = 0; i < nmodes; ++i) {
+        do {
+            for (int d = 0; d < 3; ++d) m[i].k[d] = (double)((int)(rng_uniform(r) * (2 * kmax + 1)) - kmax);
+        } while (m[i].k[0] == 0 && m[i].k[1] == 0 && m[i].k[2] == 0);
+        m[i].phase = 2.0 * M_PI * rng_uniform(r);
+        for (int d = 0; d < 3; ++d) m[i].amp[d] = amp_sigma * rng_normal(r);
+    }
+}
+static int sod_to_nat(int P, int s) { return s == 0 ? 0 : (s == 1 ? P : s - 1); }
+
+/* nx*ny*nz hexes of the unit cube, lexicographic elements and nodes
+ * ((nx P + 1)(ny P + 1)(nz P + 1) shared nodes); interior vertices of the
+ * (n+1)^3 grid jittered by up to +-jitter*h per component (a draw per vertex
+ * and component, seed-stable), high-order nodes placed at the GLL points of
+ * the trilinear map of the element's vertices.  Returns 0 on success. */
+int F(orc_mesh_structured)(int P, int nx, int ny, int nz, const int *AtoI, const int *AtoJ, const int *AtoK,
+                           double jitter, uint64_t seed, int *connec, real *coord)
+{
+    const int Q = P + 1, n = Q * Q * Q;
+    const int64_t NX = (int64_t)nx * P + 1, NY = (int64_t)ny * P + 1, NZ = (int64_t)nz * P + 1;
+    const int64_t nelem = (int64_t)nx * ny * nz, npoin = NX * NY * NZ;
+    int ni[ORC_MAXN], nj[ORC_MAXN], nk[ORC_MAXN];
+    if (P < 1 || P > ORC_MAXP) return 1;
+    for (int a = 0; a < n; ++a) {
+        ni[a] = sod_to_nat(P, AtoI[a] - 1);
+        nj[a] = sod_to_nat(P, AtoJ[a] - 1);
+        nk[a] = sod_to_nat(P, AtoK[a] - 1);
+    }
+    for (int64_t e = 0; e < nelem; ++e) {
+        const int64_t ex = e % nx, ey = (e / nx) % ny, ez = e / ((int64_t)nx * ny);
+        for (int a = 0; a < n; ++a) {
+            const int64_t I = ex * P + ni[a], J = ey * P + nj[a], K = ez * P + nk[a];
+            connec[(int64_t)a * nelem + e] = (int)((K * NY + J) * NX + I + 1);
+        }
+    }
+    if (!coord) return 0;
+    const int64_t VX = nx + 1, VY = ny + 1, VZ = nz + 1;
+    double *vx = (double *)malloc(sizeof(double) * (size_t)(VX * VY * VZ * 3));
+    if (!vx) return 2;
+    orc_rng rng = {seed ^ 0x6A09E667F3BCC908ull};
+    const double h[3] = {1.0 / nx, 1.0 / ny, 1.0 / nz};
+    for (int64_t k = 0; k < VZ; ++k)
+        for (int64_t j = 0; j < VY; ++j)
+            for (int64_t i = 0; i < VX; ++i) {
+                const int64_t v = (k * VY + j) * VX + i;
+                const int64_t idx[3] = {i, j, k}, lim[3] = {nx, ny, nz};
+                for (int d = 0; d < 3; ++d) {
+                    double x = (double)idx[d] * h[d];
+                    const double r = 2.0 * rng_uniform(&rng) - 1.0;
+                    if (idx[d] > 0 && idx[d] < lim[d]) x += jitter * h[d] * r;
+                    vx[v * 3 + d] = x;
+                }
+            }
+    double xg[ORC_MAXQ], vn[ORC_MAXQ];
+    F(orc_zelegl)(P, xg, vn); /* FP32 build: Newton starts from the FP32 pi, as the tables */
+    for (int64_t K = 0; K < NZ; ++K)
+        for (int64_t J = 0; J < NY; ++J)
+            for (int64_t I = 0; I < NX; ++I) {
+                const int64_t ex = I / P < nx ? I / P : nx - 1, ey = J / P < ny ? J / P : ny - 1,
+                              ez = K / P < nz ? K / P : nz - 1;
+                const double sv[3] = {xg[I - ex * P], xg[J - ey * P], xg[K - ez * P]};
+                double x[3] = {0, 0, 0};
+                for (int c = 0; c < 8; ++c) {
+                    const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+                    const double wgt = 0.125 * (1 + (cx ? sv[0] : -sv[0])) * (1 + (cy ? sv[1] : -sv[1])) *
+                                       (1 + (cz ? sv[2] : -sv[2]));
+                    const int64_t v = ((ez + cz) * VY + (ey + cy)) * VX + (ex + cx);
+                    for (int d = 0; d < 3; ++d) x[d] += wgt * vx[v * 3 + d];
+                }
+                const int64_t p = (K * NY + J) * NX + I;
+                for (int d = 0; d < 3; ++d) coord[d * npoin + p] = (real)x[d];
+            }
+    free(vx);
+    return 0;
+}
+
+/* Seeded node fields: kind 0 (smooth) rho = 1 + 0.1 sin sin sin, pr = 1 +
+ * 0.05 cos(2 pi x); kind 1 (shock-like) rho = 1 + 0.5 tanh((x-1/2)/0.02) + 5 %
+ * Fourier noise, uniform pressure for Mach 0.8 at the velocity scale; u a sum of
+ * nmodes Fourier modes per component (sigma 0.1 / 0.3); q = rho u; E =
+ * pr/(gamma-1)/rho + |u|^2/2; Tem = pr/(rho Rgas); mu_fluid = 1.8e-5. */
+int F(orc_fields_recipe)(int kind, int nmodes, uint64_t seed, int64_t npoin, const real *coord, real *rho, real *u,
+                         real *q, real *pr, real *E, real *Tem, real *mu_fluid)
+{
+    const double gamma = 1.4, Rgas = 287.0, tpi = 2.0 * M_PI;
+    const double uamp = kind == 0 ? 0.1 : 0.3;
+    orc_mode um[3][64], noise[64];
+    if ((kind != 0 && kind != 1) || nmodes < 1 || nmodes > 64) return 1;
+    orc_rng rng = {seed};
+    for (int c = 0; c < 3; ++c) make_modes(&rng, nmodes, 2, uamp, um[c]);
+    make_modes(&rng, nmodes, 3, 1.0, noise);
+    double noise_norm = 0.0;
+    for (int i = 0; i < nmodes; ++i) noise_norm += fabs(noise[i].amp[0]);
+    if (noise_norm <= 0.0) noise_norm = 1.0;
+    const double urms = sqrt(3.0 * nmodes * 0.5) * uamp;
+    const double p_shock = urms * urms / (gamma * 0.8 * 0.8);
+    for (int64_t p = 0; p < npoin; ++p) {
+        const double x = coord[p], y = coord[npoin + p], z = coord[2 * npoin + p];
+        double uu[3];
+        for (int c = 0; c < 3; ++c) {
+            double s = 0.0;
+            for (int i = 0; i < nmodes; ++i) {
+                const orc_mode *m = &um[c][i];
+                s += m->amp[0] * sin(tpi * (m->k[0] * x + m->k[1] * y + m->k[2] * z) + m->phase);
+            }
+            uu[c] = s;
+        }
+        double r, pp;
+        if (kind == 0) {
+            r = 1.0 + 0.1 * sin(tpi * x) * sin(tpi * y) * sin(tpi * z);
+            pp = 1.0 + 0.05 * cos(tpi * x);
+        } else {
+            double nzv = 0.0;
+            for (int i = 0; i < nmodes; ++i) {
+                const orc_mode *m = &noise[i];
+                nzv += m->amp[0] * sin(tpi * (m->k[0] * x + m->k[1] * y + m->k[2] * z) + m->phase);
+            }
+            r = 1.0 + 0.5 * tanh((x - 0.5) / 0.02) + 0.05 * nzv / noise_norm;
+            pp = p_shock;
+        }
+        const float rf = (float)r, pf = (float)pp;
+        const float uf[3] = {(float)uu[0], (float)uu[1], (float)uu[2]};
+        rho[p] = rf;
+        pr[p] = pf;
+        for (int c = 0; c < 3; ++c) {
+            u[c * npoin + p] = uf[c];
+            q[c * npoin + p] = rf * uf[c];
+        }
+        const float ke = 0.5f * (uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2]);
+        E[p] = pf / (float)(gamma - 1.0) / rf + ke;
+        Tem[p] = pf / (rf * (float)Rgas);
+        mu_fluid[p] = 1.8e-5f;
+    }
+    return 0;
+}
+#endif /* ORC_IS_FLOAT */

@@ -120,6 +120,37 @@ def create_mesh_disconnected(P, nelem, xgp, dtype=np.float32):
     return connec, coord
 
 
+def structured_mesh(P, nx, tables, jitter=0.0, seed=0):
+    """The benchmark workloads' structured shared-node mesh of the unit cube (nx^3 hexes):
+    (connec[a*nelem+e] int32 1-based, coord[d*npoin+p] float32, nelem, npoin)."""
+    n = (P + 1) ** 3
+    nelem = nx ** 3
+    npoin = (nx * P + 1) ** 3
+    connec = np.zeros(nelem * n, np.int32)
+    coord = np.zeros(3 * npoin, np.float32)
+    f = lib().orc_mesh_structured_f32
+    f.argtypes = [C.c_int] * 4 + [C.c_void_p] * 3 + [C.c_double, C.c_uint64, C.c_void_p, C.c_void_p]
+    rc = f(P, nx, nx, nx, _p(_c(tables["AtoI"], np.int32)), _p(_c(tables["AtoJ"], np.int32)),
+           _p(_c(tables["AtoK"], np.int32)), float(jitter), int(seed) & (2 ** 64 - 1), _p(connec), _p(coord))
+    if rc:
+        raise ValueError("orc_mesh_structured failed (%d)" % rc)
+    return connec, coord, nelem, npoin
+
+
+def fields_recipe(kind, nmodes, seed, npoin, coord):
+    """The benchmark workloads' seeded node fields (FP32): dict of rho, u, q, pr, E, Tem, mu_fluid."""
+    f = {k: np.zeros(npoin, np.float32) for k in ("rho", "pr", "E", "Tem", "mu_fluid")}
+    f["u"] = np.zeros(3 * npoin, np.float32)
+    f["q"] = np.zeros(3 * npoin, np.float32)
+    fn = lib().orc_fields_recipe_f32
+    fn.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_int64] + [C.c_void_p] * 8
+    rc = fn(int(kind), int(nmodes), int(seed) & (2 ** 64 - 1), int(npoin), _p(_c(coord, np.float32)),
+            _p(f["rho"]), _p(f["u"]), _p(f["q"]), _p(f["pr"]), _p(f["E"]), _p(f["Tem"]), _p(f["mu_fluid"]))
+    if rc:
+        raise ValueError("orc_fields_recipe failed (%d)" % rc)
+    return f
+
+
 def reference_ic(P, nelem, npoin, connec, dtype=np.float32):
     n = (P + 1) ** 3
     f = {k: np.zeros(npoin, dtype) for k in ("rho", "pr", "E", "Tem", "mu_fluid")}

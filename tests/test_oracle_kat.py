@@ -264,3 +264,24 @@ def test_openmp_matches_serial():
     b = O.full_convec_ijk(P, ne, npn, geom, f["u"], f["q"], f["rho"], f["pr"], f["E"], np.float64, nthreads=4)
     for x, y in zip(a, b):
         assert refimpl.rel_l2(x, y) < 1e-13
+
+
+@pytest.mark.parametrize("P,nx,jitter,kind,nmodes,seed", [(4, 5, 0.05, 0, 8, 0), (5, 4, 0.05, 1, 8, 2024),
+                                                           (7, 3, 0.05, 0, 16, 3), (2, 6, 0.0, 1, 8, 7)])
+def test_oracle_workload_recipe_equals_library(P, nx, jitter, kind, nmodes, seed):
+    """The oracle's restatement of the structured mesh and seeded fields (used by the benchmark's
+    reference arm, which loads no product code) gives the library's setup bit for bit."""
+    from minisod2d_gb300 import fem
+
+    t = O.element_tables(P)
+    c1, x1, ne1, np1 = O.structured_mesh(P, nx, t, jitter, seed)
+    tl = fem.element_tables(P)
+    c2, x2, ne2, np2 = fem.structured_mesh(P, nx, nx, nx, tl, jitter, seed)
+    assert (ne1, np1) == (ne2, np2)
+    assert np.array_equal(c1, c2)
+    assert np.array_equal(x1.view(np.uint32), x2.view(np.uint32))
+    f1 = O.fields_recipe(kind, nmodes, seed, np1, x1)
+    f2 = fem.fields_recipe(kind, nmodes, seed, np2, x2)
+    assert set(f1) == set(f2)
+    for k in f1:
+        assert np.array_equal(f1[k].view(np.uint32), f2[k].view(np.uint32)), k
