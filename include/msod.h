@@ -212,8 +212,10 @@ int msod_check_element_tables(int porder, int nelem, int npoin, const int *conne
  * status word in a static device array that stays resident on every GPU that
  * loads the library.  Limits are those of the kernel calls (porder <=
  * MSOD_MAX_PORDER, nelem*nnode < 2^31); larger sizes are rejected with
- * MSOD_ERR_PORDER / MSOD_ERR_INVALID_ARG.  The first call on a device looks up
- * the word's device address and should come before any stream capture.
+ * MSOD_ERR_PORDER / MSOD_ERR_INVALID_ARG.  Every call is synchronous: it
+ * reads the verdict back to the host and synchronises the stream, so it must
+ * not be made on a capturing stream or while a global-mode capture is under
+ * way (its first call on a device also looks up the word's device address).
  * Calls share the word: calls that overlap on the GPU race and must be
  * serialised by the caller. */
 int msod_check_element_tables_noalloc(int porder, int nelem, int npoin, const int *connec,
@@ -372,14 +374,15 @@ int msod_mlp_destroy(msod_mlp *m);
 /* Adam over nsamples device pairs (feat[nsamples*12], target[nsamples] =
  * y = nu/nu_max of the plain estimator).  The network's output s is a number
  * of decades (y = 10^-s); the loss is the mean-squared error of s against
- * -log10(max(target, 1e-12)).  Batch samples are drawn per step from `seed`;
- * the feature normalisation and training ranges are set from the training
- * data.  loss_host (steps floats) may be NULL.  Synchronous. */
-int msod_mlp_train(msod_mlp *m, const float *feat, const float *target, int nsamples, int steps,
-                   int batch, float lr, uint64_t seed, float *loss_host, void *stream);
-/* Batch gradient of the loss at the current weights (for gradient checks). */
-int msod_mlp_gradient(msod_mlp *m, const float *feat, const float *target, const int *idx, int batch,
-                      float *grad_host, void *stream);
+ * -log10(max(target, 1e-12)), each sample weighted by weight[i] (a device
+ * array; NULL: all 1).  Batch samples are drawn per step from `seed`; the
+ * feature normalisation and training ranges are set from the training data.
+ * loss_host (steps floats) may be NULL.  Synchronous. */
+int msod_mlp_train(msod_mlp *m, const float *feat, const float *target, const float *weight, int nsamples,
+                   int steps, int batch, float lr, uint64_t seed, float *loss_host, void *stream);
+/* Batch gradient of the (weighted) loss at the current weights (for gradient checks). */
+int msod_mlp_gradient(msod_mlp *m, const float *feat, const float *target, const float *weight,
+                      const int *idx, int batch, float *grad_host, void *stream);
 int msod_mlp_get_params(const msod_mlp *m, float *params_host, float *norm_host);
 int msod_mlp_set_params(msod_mlp *m, const float *params_host, const float *norm_host);
 /* y = 10^-s in (0, 1] from the network output s >= 0, nu = y*numax (if numax

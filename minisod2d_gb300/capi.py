@@ -78,8 +78,8 @@ SIGNATURES = {
     "msod_mlp_features": [_i, _i, _i] + [_p] * 8 + [_p, _p, _p, _f, _f, _f, _p, _p, _p],
     "msod_mlp_create": [C.POINTER(_p), _u64],
     "msod_mlp_destroy": [_p],
-    "msod_mlp_train": [_p, _p, _p, _i, _i, _i, _f, _u64, _p, _p],
-    "msod_mlp_gradient": [_p, _p, _p, _p, _i, _p, _p],
+    "msod_mlp_train": [_p, _p, _p, _p, _i, _i, _i, _f, _u64, _p, _p],
+    "msod_mlp_gradient": [_p, _p, _p, _p, _p, _i, _p, _p],
     "msod_mlp_get_params": [_p, _p, _p],
     "msod_mlp_set_params": [_p, _p, _p],
     "msod_mlp_predict": [_p, _p, _p, _i, _p, _p, _p, _p],

@@ -41,6 +41,10 @@ TableScratch *device_tables(int porder)
     if (!g_tables[dev]) {
         void *p = nullptr;
         if (cudaMalloc(&p, sizeof(TableScratch) * (MSOD_MAX_PORDER + 1)) != cudaSuccess) return nullptr;
+        if (cudaMemset(p, 0, sizeof(TableScratch) * (MSOD_MAX_PORDER + 1)) != cudaSuccess) {
+            cudaFree(p);
+            return nullptr;
+        }
         g_tables[dev] = static_cast<TableScratch *>(p);
     }
     return g_tables[dev] + porder;
@@ -117,6 +121,23 @@ static int run_check(int porder, int nelem, int npoin, const int *connec, const 
     return MSOD_OK;
 }
 
+// Checked mode, after a kernel: synchronise, then report (and clear) a bounded
+// wait of the kernel that ran out.
+static int check_wait_fault(TableScratch *tabs, cudaStream_t st, const char *what)
+{
+    int rc = cuda_status(cudaStreamSynchronize(st), what);
+    if (rc) return rc;
+    int h = 0;
+    rc = cuda_status(cudaMemcpy(&h, &tabs->wait_fault, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
+    if (rc) return rc;
+    if (h) {
+        cudaMemset(&tabs->wait_fault, 0, sizeof(int));
+        return set_error(MSOD_ERR_CUDA, "%s: a bulk copy into shared memory did not complete in time; "
+                                        "the residuals are incomplete", what);
+    }
+    return MSOD_OK;
+}
+
 template <typename real>
 static int zero_outputs(real *Rmass, real *Rmom, real *Rener, int npoin, cudaStream_t st)
 {
@@ -153,7 +174,7 @@ static int convec_impl(int porder, int nelem, int npoin, const int *connec, cons
     a.u = u; a.q = q; a.rho = rho; a.pr = pr; a.E = E; a.Rmass = Rmass; a.Rmom = Rmom; a.Rener = Rener;
     rc = cuda_status(launch_table_prep<real>(porder, a, tabs, st), "table preparation launch");
     if (!rc) rc = cuda_status(launch_convec_plain<real>(porder, a, tabs, st), "convection kernel launch");
-    if (!rc && checked_mode()) rc = cuda_status(cudaStreamSynchronize(st), "convection kernel");
+    if (!rc && checked_mode()) rc = check_wait_fault(tabs, st, "convection kernel");
     return rc;
 }
 
@@ -187,7 +208,7 @@ static int diffu_impl(int porder, int nelem, int npoin, const int *connec, const
     a.Rmass = Rmass; a.Rmom = Rmom; a.Rener = Rener;
     rc = cuda_status(launch_table_prep<real>(porder, a, tabs, st), "table preparation launch");
     if (!rc) rc = cuda_status(launch_diffu_plain<real>(porder, a, tabs, st), "diffusion kernel launch");
-    if (!rc && checked_mode()) rc = cuda_status(cudaStreamSynchronize(st), "diffusion kernel");
+    if (!rc && checked_mode()) rc = check_wait_fault(tabs, st, "diffusion kernel");
     return rc;
 }
 

@@ -90,6 +90,25 @@ __constant__ float2 c_CDp[MSOD_MAX_PORDER + 1][kTableDPairMax / 2];
 #define CONVEC_X2 1
 #endif
 
+// Threads take their lines from the bank-aware map (LineMap) with one thread
+// per line, up to this porder (0: never); other porders keep the lines of
+// consecutive elements side by side.  Measured with the three full-matrix
+// passes: plain_64 1.611 against 1.640 ms; porder 5 on 64^3 hexes 3.01
+// either way.
+#ifndef CONVEC_LINEMAP
+#define CONVEC_LINEMAP 4
+#endif
+
+// The thread's line in direction dir.
+template <class G>
+__device__ __forceinline__ LineThread<G> convec_line(int tid, int dir)
+{
+    if constexpr (G::P <= CONVEC_LINEMAP && G::S == 1)
+        return LineThread<G>(kLineMap<G>.code[dir][tid], true);
+    else
+        return LineThread<G>(tid);
+}
+
 template <int Q, typename real>
 __device__ __forceinline__ real pick(const real (&a)[Q], int i)
 {
@@ -102,7 +121,7 @@ __device__ __forceinline__ real pick(const real (&a)[Q], int i)
 enum { F_RHO = 0, F_P, F_E, F_U0, F_U1, F_U2, F_Q0, F_Q1, F_Q2, NFIELD };
 enum { A_M = 0, A_MOM0, A_MOM1, A_MOM2, A_E, A_DIVU, A_DIVQ, NACC };
 
-template <typename real, int P, int DIR>
+template <typename real, int P, int DIR, bool STAGED>
 __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *__restrict__ sA,
                                             const real *__restrict__ sD, const int *__restrict__ sNode,
                                             const int *__restrict__ sPerm, const real *__restrict__ He,
@@ -115,12 +134,9 @@ __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *_
     constexpr int NPL = NE * ES;
     constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
 
-    const int tid = threadIdx.x;
-    if (tid >= NE * TPE) return;
-    const int el = tid / TPE, rem = tid - el * TPE;
-    const int line = S == 1 ? rem : rem / S;
-    const int seg = S == 1 ? 0 : rem - line * S;
-    const int la = line % Q, lb = line / Q;
+    const LineThread<G> lt = convec_line<G>(threadIdx.x, DIR);
+    if (!lt.active) return;
+    const int el = lt.el, la = lt.la, lb = lt.lb;
     const int e = e0 + el;
     const int base = el * ES + line_off<DIR, Q, QP>(la, lb, 0);
 
@@ -143,7 +159,7 @@ __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *_
     }
 
     // Per owned point: derivative-matrix row, He column DIR, coefficients.
-    const int r0 = seg * R;
+    const int r0 = lt.r0;
     real Dm[R][Q], h[R][3], own_rho[R], own_H[R], own_rH[R], own_u[R][3], own_q[R][3], cu[R], cq[R];
     real acc[R][NACC];
     int gidx[R];
@@ -157,9 +173,9 @@ __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *_
             for (int c = 0; c < Q; ++c) Dm[rr][c] = sD[(DIR * Q + rc) * Q + c];
         const int a = sPerm[line_lat<DIR, Q>(la, lb, rc)];
         gidx[rr] = a;
-        const real *hp = He + ((size_t)(e < nelem ? e : 0) * N + a) * 9 + DIR * 3;
+        const real *hp = STAGED ? He + (el * N + a) * 9 + DIR * 3 : He + ((size_t)(e < nelem ? e : 0) * N + a) * 9 + DIR * 3;
 #pragma unroll
-        for (int i = 0; i < 3; ++i) h[rr][i] = ldg(hp + i);
+        for (int i = 0; i < 3; ++i) h[rr][i] = STAGED ? hp[i] : ldg(hp + i);
         own_rho[rr] = pick<Q>(rho_, rc);
         own_H[rr] = pick<Q>(H_, rc);
         own_rH[rr] = pick<Q>(rH_, rc);
@@ -284,7 +300,7 @@ __device__ __forceinline__ void convec_pass(const real *__restrict__ sF, real *_
             const int node = sNode[o];
             if (node < 0 || e >= nelem) continue;
             const real divU = acc[rr][A_DIVU], divQ = acc[rr][A_DIVQ];
-            const real gp = ldg(gpvol + (size_t)e * N + gidx[rr]);
+            const real gp = STAGED ? gpvol[el * N + gidx[rr]] : ldg(gpvol + (size_t)e * N + gidx[rr]);
             const real rm = acc[rr][A_M] + h2 * (divQ + own_rho[rr] * divU);
             const real re = acc[rr][A_E] + h4 * (own_H[rr] * divQ + own_rH[rr] * divU);
             red_add(Rmass + node, gp * rm);
@@ -306,7 +322,7 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 // per instruction: rows (2m, 2m+1) are the two halves of fma.rn.f32x2 /
 // mul.rn.f32x2 operands, operation for operation the scalar pass (a line of
 // odd length pads its last pair with a zero row that is never stored).
-template <int P, int DIR>
+template <int P, int DIR, bool STAGED>
 __device__ __forceinline__ void convec_pass_x2(const float *__restrict__ sF, float *__restrict__ sA,
                                                const int *__restrict__ sNode, const int *__restrict__ sPerm,
                                                const float *__restrict__ He, const float *__restrict__ gpvol, int e0,
@@ -320,10 +336,9 @@ __device__ __forceinline__ void convec_pass_x2(const float *__restrict__ sF, flo
     constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
     static_assert(G::S == 1, "one thread per line");
 
-    const int tid = threadIdx.x;
-    if (tid >= NE * TPE) return;
-    const int el = tid / TPE, line = tid - el * TPE;
-    const int la = line % Q, lb = line / Q;
+    const LineThread<G> lt = convec_line<G>(threadIdx.x, DIR);
+    if (!lt.active) return;
+    const int el = lt.el, la = lt.la, lb = lt.lb;
     const int e = e0 + el;
     const int base = el * ES + line_off<DIR, Q, QP>(la, lb, 0);
 
@@ -357,9 +372,10 @@ __device__ __forceinline__ void convec_pass_x2(const float *__restrict__ sF, flo
             if (r < Q) {
                 const int a = sPerm[line_lat<DIR, Q>(la, lb, r)];
                 gidx[r] = a;
-                const float *hp = He + ((size_t)(e < nelem ? e : 0) * N + a) * 9 + DIR * 3;
+                const float *hp = STAGED ? He + (el * N + a) * 9 + DIR * 3
+                                         : He + ((size_t)(e < nelem ? e : 0) * N + a) * 9 + DIR * 3;
 #pragma unroll
-                for (int i = 0; i < 3; ++i) hv[t][i] = ldg(hp + i);
+                for (int i = 0; i < 3; ++i) hv[t][i] = STAGED ? hp[i] : ldg(hp + i);
             } else {
                 gidx[r] = 0;
 #pragma unroll
@@ -491,7 +507,7 @@ __device__ __forceinline__ void convec_pass_x2(const float *__restrict__ sF, flo
             const int node = sNode[o];
             if (node < 0 || e >= nelem) continue;
             const float divU = a[A_DIVU], divQ = a[A_DIVQ];
-            const float gp = ldg(gpvol + (size_t)e * N + gidx[r]);
+            const float gp = STAGED ? gpvol[el * N + gidx[r]] : ldg(gpvol + (size_t)e * N + gidx[r]);
             const float rm = a[A_M] + 0.5f * (divQ + rho_[r] * divU);
             const float re = a[A_E] + 0.25f * (H_[r] * divQ + rH_[r] * divU);
             red_add(Rmass + node, gp * rm);
@@ -505,6 +521,240 @@ __device__ __forceinline__ void convec_pass_x2(const float *__restrict__ sF, flo
     }
 }
 
+// ---------------------------------------------------------------------------
+// The compact pass (FP32, one thread per line, scalar porders): one copy of
+// the pass code serves the three directions (the direction is a run-time
+// value), and the contraction takes the even-odd form of the derivative
+// matrix.  Both need what the reference's tables provide: one 1-D matrix for
+// the three directions, centro-antisymmetric (table_prep_kernel checks it per
+// call, TableScratch::eo_ok); other tables take the three unrolled passes.
+// ---------------------------------------------------------------------------
+// 1 = even-odd contraction (porder 4: 20 instead of 25 FP32 operations per
+// line and field), 0 = the full matrix of direction 0.  Measured on plain_64
+// (unrolled passes, four blocks per SM): 1.48 ms against 1.62 ms for the
+// three full-matrix passes; porder 2 on 120^3 hexes 1.71 against 1.79 ms.
+#ifndef CONVEC_EO
+#define CONVEC_EO 1
+#endif
+// 1 = the direction loop is not unrolled (one copy of the pass code: a third
+// of the instruction footprint), 0 = unrolled.  Measured on plain_64: the
+// run-time direction loses (1.80 ms at four blocks per SM, 1.60 ms at three)
+// against the unrolled passes (1.48 ms): the kernel is not bound by
+// instruction fetch.
+#ifndef CONVEC_RTDIR
+#define CONVEC_RTDIR 0
+#endif
+// 1 = the compact pass runs when the call's tables allow it, 0 = never.
+#ifndef CONVEC_COMPACT
+#define CONVEC_COMPACT 1
+#endif
+
+__constant__ float c_CEO[MSOD_MAX_PORDER + 1][kTableEOMax];
+
+template <int Q, int QP>
+__device__ __forceinline__ int line_off_rt(int dir, int la, int lb, int r)
+{
+    return dir == 0 ? (lb * Q + la) * QP + r : (dir == 1 ? (lb * Q + r) * QP + la : (r * Q + lb) * QP + la);
+}
+template <int Q>
+__device__ __forceinline__ int line_lat_rt(int dir, int la, int lb, int r)
+{
+    return line_off_rt<Q, Q>(dir, la, lb, r);
+}
+
+template <int P>
+__device__ __forceinline__ void convec_pass_compact(int dir, const float *__restrict__ sF, float *__restrict__ sA,
+                                                    const int *__restrict__ sNode, const int *__restrict__ sPerm,
+                                                    const float *__restrict__ He, const float *__restrict__ gpvol,
+                                                    int e0, int nelem, int npoin, float *__restrict__ Rmass,
+                                                    float *__restrict__ Rmom, float *__restrict__ Rener)
+{
+    using G = ConvecGeom<float, P>;
+    constexpr int Q = G::Q, QP = G::QP, ES = G::ES, N = G::N, NPL = G::NE * G::ES;
+    constexpr int M = Q / 2, MC = sod_centre(Q);
+    constexpr bool ODD = (Q % 2) == 1;
+    static_assert(G::S == 1, "one thread per line");
+    const LineThread<G> lt = convec_line<G>(threadIdx.x, dir);
+    if (!lt.active) return;
+    const int el = lt.el, la = lt.la, lb = lt.lb;
+    const int e = e0 + el;
+    const int ost = dir == 0 ? 1 : (dir == 1 ? QP : Q * QP);
+    const int base = el * ES + line_off_rt<Q, QP>(dir, la, lb, 0);
+
+    float rho_[Q], p_[Q], H_[Q], rH_[Q], u_[3][Q], q_[3][Q];
+#pragma unroll
+    for (int c = 0; c < Q; ++c) {
+        const int o = base + c * ost;
+        rho_[c] = sF[F_RHO * NPL + o];
+        p_[c] = sF[F_P * NPL + o];
+        const float Ev = sF[F_E * NPL + o];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            u_[i][c] = sF[(F_U0 + i) * NPL + o];
+            q_[i][c] = sF[(F_Q0 + i) * NPL + o];
+        }
+        const float k = 0.5f * (u_[0][c] * u_[0][c] + u_[1][c] * u_[1][c] + u_[2][c] * u_[2][c]);
+        H_[c] = Ev + k;
+        rH_[c] = rho_[c] * H_[c];
+    }
+
+    float h[Q][3], cu[Q], cq[Q], acc[Q][NACC];
+    int gidx[Q];
+#pragma unroll
+    for (int r = 0; r < Q; ++r) {
+        const int a = sPerm[line_lat_rt<Q>(dir, la, lb, r)];
+        gidx[r] = a;
+        const float *hp = He + ((size_t)(e < nelem ? e : 0) * N + a) * 9 + dir * 3;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) h[r][i] = ldg(hp + i);
+        cu[r] = u_[0][r] * h[r][0] + u_[1][r] * h[r][1] + u_[2][r] * h[r][2];
+        cq[r] = q_[0][r] * h[r][0] + q_[1][r] * h[r][1] + q_[2][r] * h[r][2];
+        const int o = base + r * ost;
+#pragma unroll
+        for (int k = 0; k < NACC; ++k) acc[r][k] = dir == 0 ? 0.0f : sA[k * NPL + o];
+    }
+
+    float d[Q], f[Q];
+    auto deriv = [&](const float(&v)[Q]) {
+        if constexpr (CONVEC_EO != 0) {
+            float ev[M > 0 ? M : 1], od[M > 0 ? M : 1];
+#pragma unroll
+            for (int j = 0; j < M; ++j) {
+                ev[j] = v[sod_left(j)] + v[sod_mirror(Q, sod_left(j))];
+                od[j] = v[sod_left(j)] - v[sod_mirror(Q, sod_left(j))];
+            }
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                float sO = 0.0f, sE = ODD ? c_CEO[P][2 * M * M + i] * v[MC] : 0.0f;
+#pragma unroll
+                for (int j = 0; j < M; ++j) {
+                    sO = fmaf(c_CEO[P][i * M + j], od[j], sO);
+                    sE = fmaf(c_CEO[P][M * M + i * M + j], ev[j], sE);
+                }
+                d[sod_left(i)] = sO + sE;
+                d[sod_mirror(Q, sod_left(i))] = sO - sE;
+            }
+            if constexpr (ODD) {
+                float sm = 0.0f;
+#pragma unroll
+                for (int j = 0; j < M; ++j) sm = fmaf(c_CEO[P][2 * M * M + M + j], od[j], sm);
+                d[MC] = sm;
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < Q; ++r) {
+                float sd = 0.0f;
+#pragma unroll
+                for (int c = 0; c < Q; ++c) sd = fmaf(cCD<float>(P, r * Q + c), v[c], sd);
+                d[r] = sd;
+            }
+        }
+    };
+
+    // rho: mass 1/2 u.grad rho, momentum 1/4 u_i u.grad rho, energy 1/4 H u.grad rho
+    deriv(rho_);
+#pragma unroll
+    for (int r = 0; r < Q; ++r) {
+        const float t4 = 0.25f * (cu[r] * d[r]);
+        acc[r][A_M] = fmaf(2.0f, t4, acc[r][A_M]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) acc[r][A_MOM0 + i] = fmaf(u_[i][r], t4, acc[r][A_MOM0 + i]);
+        acc[r][A_E] = fmaf(H_[r], t4, acc[r][A_E]);
+    }
+    // p: grad p
+    deriv(p_);
+#pragma unroll
+    for (int r = 0; r < Q; ++r)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) acc[r][A_MOM0 + i] = fmaf(h[r][i], d[r], acc[r][A_MOM0 + i]);
+    // u_i: div u, 1/4 q.grad u_i ; q_i: div q, 1/4 u.grad q_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        deriv(u_[i]);
+#pragma unroll
+        for (int r = 0; r < Q; ++r) {
+            acc[r][A_DIVU] = fmaf(h[r][i], d[r], acc[r][A_DIVU]);
+            acc[r][A_MOM0 + i] = fmaf(0.25f * cq[r], d[r], acc[r][A_MOM0 + i]);
+        }
+        deriv(q_[i]);
+#pragma unroll
+        for (int r = 0; r < Q; ++r) {
+            acc[r][A_DIVQ] = fmaf(h[r][i], d[r], acc[r][A_DIVQ]);
+            acc[r][A_MOM0 + i] = fmaf(0.25f * cu[r], d[r], acc[r][A_MOM0 + i]);
+        }
+    }
+    // F_ij = q_i u_j: 1/4 div F_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+#pragma unroll
+            for (int c = 0; c < Q; ++c) f[c] = q_[i][c] * u_[j][c];
+            deriv(f);
+#pragma unroll
+            for (int r = 0; r < Q; ++r) acc[r][A_MOM0 + i] = fmaf(0.25f * h[r][j], d[r], acc[r][A_MOM0 + i]);
+        }
+    // Fuu_ij = u_i u_j (symmetric): 1/4 rho div Fuu_i
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = i; j < 3; ++j) {
+#pragma unroll
+            for (int c = 0; c < Q; ++c) f[c] = u_[i][c] * u_[j][c];
+            deriv(f);
+#pragma unroll
+            for (int r = 0; r < Q; ++r) {
+                const float rd = (0.25f * rho_[r]) * d[r];
+                acc[r][A_MOM0 + i] = fmaf(h[r][j], rd, acc[r][A_MOM0 + i]);
+                if (i != j) acc[r][A_MOM0 + j] = fmaf(h[r][i], rd, acc[r][A_MOM0 + j]);
+            }
+        }
+    // H: 1/4 q.grad H ; rho H: 1/4 u.grad(rho H)
+    deriv(H_);
+#pragma unroll
+    for (int r = 0; r < Q; ++r) acc[r][A_E] = fmaf(0.25f * cq[r], d[r], acc[r][A_E]);
+    deriv(rH_);
+#pragma unroll
+    for (int r = 0; r < Q; ++r) acc[r][A_E] = fmaf(0.25f * cu[r], d[r], acc[r][A_E]);
+    // rho H u_i: 1/4 div(rho H u) ; H u_i: 1/4 rho div(H u)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = rH_[c] * u_[i][c];
+        deriv(f);
+#pragma unroll
+        for (int r = 0; r < Q; ++r) acc[r][A_E] = fmaf(0.25f * h[r][i], d[r], acc[r][A_E]);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) f[c] = H_[c] * u_[i][c];
+        deriv(f);
+#pragma unroll
+        for (int r = 0; r < Q; ++r) acc[r][A_E] = fmaf((0.25f * rho_[r]) * h[r][i], d[r], acc[r][A_E]);
+    }
+
+#pragma unroll
+    for (int r = 0; r < Q; ++r) {
+        const int o = base + r * ost;
+        if (dir < 2) {
+#pragma unroll
+            for (int k = 0; k < NACC; ++k) sA[k * NPL + o] = acc[r][k];
+        } else {
+            const int node = sNode[o];
+            if (node < 0 || e >= nelem) continue;
+            const float divU = acc[r][A_DIVU], divQ = acc[r][A_DIVQ];
+            const float gp = ldg(gpvol + (size_t)e * N + gidx[r]);
+            const float rm = acc[r][A_M] + 0.5f * (divQ + rho_[r] * divU);
+            const float re = acc[r][A_E] + 0.25f * (H_[r] * divQ + rH_[r] * divU);
+            red_add(Rmass + node, gp * rm);
+            red_add(Rener + node, gp * re);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float rmom = acc[r][A_MOM0 + i] + 0.25f * (u_[i][r] * divQ + q_[i][r] * divU);
+                red_add(Rmom + (size_t)i * npoin + node, gp * rmom);
+            }
+        }
+    }
+}
+
 template <typename real, int P>
 constexpr bool convec_packed()
 {
@@ -512,24 +762,68 @@ constexpr bool convec_packed()
            ConvecGeom<real, P>::S == 1;
 }
 
-template <typename real, int P, int DIR>
+template <typename real, int P, int DIR, bool STAGED>
 __device__ __forceinline__ void convec_dir(const real *sF, real *sA, const real *sD, const int *sNode,
                                            const int *sPerm, const real *He, const real *gpvol, int e0, int nelem,
                                            int npoin, real *Rmass, real *Rmom, real *Rener)
 {
     if constexpr (convec_packed<real, P>())
-        convec_pass_x2<P, DIR>(sF, sA, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+        convec_pass_x2<P, DIR, STAGED>(sF, sA, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
     else
-        convec_pass<real, P, DIR>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+        convec_pass<real, P, DIR, STAGED>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom,
+                                          Rener);
+}
+
+// He and gpvol of a block's elements staged in shared memory by bulk copies
+// (the group's spans of He(3,3,ngaus,nelem) and gpvol(ngaus,nelem) are
+// contiguous): 1 = FP32 kernels, 0 = per-point loads from global memory.
+// Measured slower and off: plain_64 1.95 ms against 1.61 ms (three blocks per
+// SM by shared memory instead of four, and the gmsh-ordered He records read
+// from shared memory by line threads conflict on banks); porder 5 on 64^3
+// hexes 3.10 against 3.01 ms.
+#ifndef CONVEC_HE_BULK
+#define CONVEC_HE_BULK 0
+#endif
+template <typename real>
+constexpr bool convec_staged()
+{
+    return CONVEC_HE_BULK != 0 && sizeof(real) == 4;
+}
+// Porders whose kernels carry the compact pass (FP32, scalar line passes).
+template <typename real, int P>
+constexpr bool convec_compact_capable()
+{
+    return CONVEC_COMPACT != 0 && sizeof(real) == 4 && ConvecGeom<real, P>::S == 1 && !convec_packed<real, P>() &&
+           !convec_staged<real>();
+}
+// Bytes of the staging area: He span, gpvol span (each with 16-byte slack for
+// the unaligned start, rounded to 16) and the mbarrier.
+template <typename real, int P>
+constexpr size_t convec_stage_bytes()
+{
+    using G = ConvecGeom<real, P>;
+    return convec_staged<real>() ? ((size_t)G::NE * G::N * 9 * sizeof(real) + 31) / 16 * 16 +
+                                       ((size_t)G::NE * G::N * sizeof(real) + 31) / 16 * 16 + 16
+                                 : 0;
 }
 
 // Blocks per SM the register budget is sized for: four 128-thread blocks (128
-// registers) when the derivative matrices are constant-bank operands.
+// registers) when the derivative matrices are constant-bank operands; three
+// at porder 4 when He and gpvol are staged (their 25 KB per block leave room
+// for three blocks, so a 128-register budget would buy nothing).
+#ifndef CONVEC_MINB4_STAGED
+#define CONVEC_MINB4_STAGED 3
+#endif
+#ifndef CONVEC_MINB4
+#define CONVEC_MINB4 CONVEC_MINB
+#endif
 template <typename real, int P>
 constexpr int convec_minb()
 {
     using G = ConvecGeom<real, P>;
-    return (sizeof(real) == 4 && G::S == 1 && G::NT <= 128 && P >= 3) ? (P == 5 ? CONVEC_MINB5 : CONVEC_MINB) : 1;
+    return (sizeof(real) == 4 && G::S == 1 && G::NT <= 128 && P >= 3)
+               ? (P == 5 ? CONVEC_MINB5 : (P == 4 ? (convec_staged<real>() ? CONVEC_MINB4_STAGED : CONVEC_MINB4) : CONVEC_MINB))
+               : 1;
 }
 
 template <typename real, int P>
@@ -547,7 +841,13 @@ __global__ void __launch_bounds__(ConvecGeom<real, P>::NT, convec_minb<real, P>(
     constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT;
     constexpr int NPL = NE * ES;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    real *sF = reinterpret_cast<real *>(smem_raw);
+    constexpr bool STAGED = convec_staged<real>();
+    constexpr size_t HEB = ((size_t)NE * N * 9 * sizeof(real) + 31) / 16 * 16;
+    constexpr size_t GPB = ((size_t)NE * N * sizeof(real) + 31) / 16 * 16;
+    char *sHeB = reinterpret_cast<char *>(smem_raw);
+    char *sGpB = sHeB + HEB;
+    unsigned long long *sBar = reinterpret_cast<unsigned long long *>(sGpB + GPB);
+    real *sF = reinterpret_cast<real *>(smem_raw + convec_stage_bytes<real, P>());
     real *sA = sF + NFIELD * NPL;
     real *sD = sA + NACC * NPL;
     int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);
@@ -556,6 +856,29 @@ __global__ void __launch_bounds__(ConvecGeom<real, P>::NT, convec_minb<real, P>(
 
     const int tid = threadIdx.x;
     const int e0 = blockIdx.x * NE;
+    // The compact pass when the call's tables allow it (uniform over the grid).
+    bool compact = false;
+    if constexpr (convec_compact_capable<real, P>()) compact = ldg(&tabs->eo_ok) != 0;
+    // The group's He and gpvol spans: bulk copies issued first, so that they
+    // land while the node fields are gathered.
+    const real *Hs = He, *Gs = gpvol;
+    if constexpr (STAGED) {
+        const int e1 = min(e0 + NE, nelem);
+        const SpanPlan ph(He + (size_t)e0 * N * 9, (size_t)(e1 - e0) * N * 9 * sizeof(real));
+        const SpanPlan pg(gpvol + (size_t)e0 * N, (size_t)(e1 - e0) * N * sizeof(real));
+        if (tid == 0) {
+            mbar_init(sBar, 1);
+            mbar_arrive_expect_tx(sBar, ph.bulk + pg.bulk);
+            ph.issue(sHeB, sBar);
+            pg.issue(sGpB, sBar);
+        } else if (tid >= 32 && tid < 38) {
+            ph.plain(sHeB, tid - 32);
+        } else if (tid >= 64 && tid < 70) {
+            pg.plain(sGpB, tid - 64);
+        }
+        Hs = reinterpret_cast<const real *>(sHeB + ph.shift);
+        Gs = reinterpret_cast<const real *>(sGpB + pg.shift);
+    }
     // Node ids of the group's elements (connec is element-fastest), loaded
     // while the per-call tables are copied into shared memory.
     constexpr int IPT = (NE * N + NT - 1) / NT;
@@ -603,20 +926,43 @@ __global__ void __launch_bounds__(ConvecGeom<real, P>::NT, convec_minb<real, P>(
     }
     cp_async_commit();
     cp_async_wait_all();
+    if constexpr (STAGED) {
+        // Bounded wait for the bulk copies; every thread learns the outcome.
+        const bool ok = mbar_wait(sBar, 0);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) report_wait_fault(tabs);
+            return;
+        }
+    } else {
+        __syncthreads();
+    }
+    if constexpr (convec_compact_capable<real, P>()) {
+        if (compact) {
+#if CONVEC_RTDIR
+#pragma unroll 1
+#else
+#pragma unroll
+#endif
+            for (int dir = 0; dir < 3; ++dir) {
+                if (dir > 0) __syncthreads();
+                convec_pass_compact<P>(dir, sF, sA, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+            }
+            return;
+        }
+    }
+    convec_dir<real, P, 0, STAGED>(sF, sA, sD, sNode, sPerm, Hs, Gs, e0, nelem, npoin, Rmass, Rmom, Rener);
     __syncthreads();
-    convec_dir<real, P, 0>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+    convec_dir<real, P, 1, STAGED>(sF, sA, sD, sNode, sPerm, Hs, Gs, e0, nelem, npoin, Rmass, Rmom, Rener);
     __syncthreads();
-    convec_dir<real, P, 1>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
-    __syncthreads();
-    convec_dir<real, P, 2>(sF, sA, sD, sNode, sPerm, He, gpvol, e0, nelem, npoin, Rmass, Rmom, Rener);
+    convec_dir<real, P, 2, STAGED>(sF, sA, sD, sNode, sPerm, Hs, Gs, e0, nelem, npoin, Rmass, Rmom, Rener);
 }
 
 template <typename real, int P>
 constexpr size_t convec_smem()
 {
     using G = ConvecGeom<real, P>;
-    return (size_t)(NFIELD + NACC) * G::NE * G::ES * sizeof(real) + 3 * G::Q * G::Q * sizeof(real) +
-           (size_t)(G::NE * G::ES + 2 * G::N) * sizeof(int);
+    return convec_stage_bytes<real, P>() + (size_t)(NFIELD + NACC) * G::NE * G::ES * sizeof(real) +
+           3 * G::Q * G::Q * sizeof(real) + (size_t)(G::NE * G::ES + 2 * G::N) * sizeof(int);
 }
 
 template <typename real, int P>
@@ -636,6 +982,11 @@ cudaError_t launch_convec_p(const ConvecArgs<real> &a, const TableScratch *tabs,
             err = cudaMemcpyToSymbolAsync(c_CDd, table_D<double>(tabs), sizeof(double) * 3 * G::Q * G::Q,
                                           sizeof(double) * kTableDMax * P, cudaMemcpyDeviceToDevice, st);
         if (err != cudaSuccess) return err;
+        if (convec_compact_capable<real, P>()) {
+            err = cudaMemcpyToSymbolAsync(c_CEO, tabs->EO, sizeof(float) * kTableEOMax, sizeof(float) * kTableEOMax * P,
+                                          cudaMemcpyDeviceToDevice, st);
+            if (err != cudaSuccess) return err;
+        }
         if (convec_packed<real, P>()) {
             constexpr int H = (G::Q + 1) / 2;
             err = cudaMemcpyToSymbolAsync(c_CDp, tabs->Dp, sizeof(float2) * 3 * G::Q * H,

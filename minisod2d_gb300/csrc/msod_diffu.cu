@@ -60,8 +60,33 @@
 #define DIFFU_NBUF 1
 #endif
 
+// Threads take their lines from the bank-aware map (LineMap) with one thread
+// per line, up to this porder (0: never); other porders keep the lines of
+// consecutive elements side by side.  Measured: plain_64 1.483 against
+// 1.503 ms; porder 5 on 64^3 hexes 2.99 against 2.96 ms (off there).
+#ifndef DIFFU_LINEMAP
+#define DIFFU_LINEMAP 4
+#endif
+// Gather of the node fields: 0 = 4-byte cp.async copies, 1 = loads into
+// registers, then 32-lane shared-memory stores.  Measured: plain_64 1.466
+// against 1.483 ms (at three blocks per SM, DIFFU_MINB4=3), porder 5 on 64^3
+// hexes 3.82 against 2.99 ms (registers); off.
+#ifndef DIFFU_GATHER_LDG
+#define DIFFU_GATHER_LDG 0
+#endif
+
 namespace msod {
 namespace {
+
+// The thread's line in direction dir.
+template <class G>
+__device__ __forceinline__ LineThread<G> diffu_line(int tid, int dir)
+{
+    if constexpr (G::P <= DIFFU_LINEMAP && G::S == 1)
+        return LineThread<G>(kLineMap<G>.code[dir][tid], true);
+    else
+        return LineThread<G>(tid);
+}
 
 __constant__ float c_Df[MSOD_MAX_PORDER + 1][kTableDMax];
 __constant__ double c_Dd[MSOD_MAX_PORDER + 1][kTableDMax];
@@ -263,10 +288,41 @@ __device__ __forceinline__ real kappa_e(real muf, real me, real ms, real r, real
     return muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
 }
 
+// He and gpvol of a group staged in shared memory by bulk copies (the group's
+// spans of He(3,3,ngaus,nelem) and gpvol(ngaus,nelem) are contiguous), issued
+// one group ahead: 1 = the fused zeta stage's FP32 kernels, 0 = per-point
+// loads from global memory.  Measured slower and off: the 25 KB per block
+// leave two blocks per SM instead of three (plain_64 1.76 against 1.48 ms;
+// porder 5 on 64^3 hexes 3.63 against 2.99 ms).
+#ifndef DIFFU_HE_BULK
+#define DIFFU_HE_BULK 0
+#endif
+template <class G>
+constexpr bool diffu_staged()
+{
+    return DIFFU_HE_BULK != 0 && diffu_fusez<G>() && DIFFU_HE_LATE != 0 && sizeof(typename G::real) == 4;
+}
+template <class G>
+constexpr size_t diffu_he_bytes()
+{
+    return ((size_t)G::NE * G::N * 9 * sizeof(typename G::real) + 31) / 16 * 16;
+}
+template <class G>
+constexpr size_t diffu_gp_bytes()
+{
+    return ((size_t)G::NE * G::N * sizeof(typename G::real) + 31) / 16 * 16;
+}
+template <class G>
+constexpr size_t diffu_stage_bytes()
+{
+    return diffu_staged<G>() ? diffu_he_bytes<G>() + diffu_gp_bytes<G>() + 16 : 0;
+}
+
 template <class G>
 constexpr size_t diffu_smem_bytes()
 {
-    return (size_t)(DIFFU_NBUF * NDF + diffu_xplanes<G>()) * G::NPL * sizeof(typename G::real) +
+    return diffu_stage_bytes<G>() +
+           (size_t)(DIFFU_NBUF * NDF + diffu_xplanes<G>()) * G::NPL * sizeof(typename G::real) +
            (size_t)3 * G::Q * G::Q * sizeof(typename G::real) +
            (size_t)(DIFFU_NBUF * G::NPL + 2 * G::N) * sizeof(int);
 }
@@ -341,7 +397,11 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     constexpr int IPT = (NE * N + NT - 1) / NT;  // items (node ids, points) per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NBUF = DIFFU_NBUF;
-    real *sF = reinterpret_cast<real *>(smem_raw);  // [NBUF][NDF][NPL]
+    constexpr bool STAGED = diffu_staged<G>();
+    char *sHeB = reinterpret_cast<char *>(smem_raw);  // staged He / gpvol spans, then the mbarrier
+    char *sGpB = sHeB + diffu_he_bytes<G>();
+    unsigned long long *sBar = reinterpret_cast<unsigned long long *>(sGpB + diffu_gp_bytes<G>());
+    real *sF = reinterpret_cast<real *>(smem_raw + diffu_stage_bytes<G>());  // [NBUF][NDF][NPL]
     real *sX = sF + NBUF * NDF * NPL;                // [2 or 3 NX][NPL]
     real *sD = sX + diffu_xplanes<G>() * NPL;        // [3][Q][Q] (several threads per line)
     int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);  // [NBUF][NPL]
@@ -352,7 +412,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     float *sInfo = sFeat + NE * kMlpIn;                   // [NE][4]: numax, flag, fallback nu, nu
 
     const int tid = threadIdx.x;
-    const LineThread<G> lt(tid);
+    const LineThread<G> lt0 = diffu_line<G>(tid, 0), lt1 = diffu_line<G>(tid, 1), lt2 = diffu_line<G>(tid, 2);
     constexpr bool FUSEZ = diffu_fusez<G>();
     constexpr bool LATE = FUSEZ && DIFFU_HE_LATE != 0;
     constexpr int MP = LATE ? 1 : (FUSEZ ? Q : IPT);  // points whose He and gpvol a thread holds
@@ -479,6 +539,46 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     };
     // Node fields in lattice order; mu_e / mu_sgs along elements (coalesced).
     auto gather = [&](int g, const int *ids_s, real *dst) {
+        if constexpr (DIFFU_GATHER_LDG != 0) {
+            // Loads of all of a thread's items first, then the stores.
+            real v[IPT][6], w[IPT][2];
+            int ov[IPT], ow[IPT];
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const int i = tid + k * NT;
+                const bool in = i < NE * N;
+                const int el = in ? i / N : 0, l = in ? i - el * N : 0;
+                const int I = l % Q, J = (l / Q) % Q, K = l / (Q * Q);
+                const int o = el * ES + (K * Q + J) * QP + I;
+                ov[k] = in ? o : -1;
+                const int p = in ? ids_s[o] : -1;
+                const bool ok = (unsigned)p < (unsigned)npoin;
+                const size_t pp = ok ? (size_t)p : 0, np = (size_t)npoin;
+                v[k][0] = ok ? ldg(rho + pp) : (real)0;
+                v[k][1] = ok ? ldg(Tem + pp) : (real)0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) v[k][2 + c] = ok ? ldg(u + c * np + pp) : (real)0;
+                v[k][5] = ok ? ldg(mu_fluid + pp) : (real)0;
+                const int el2 = i % NE, a = i / NE, e = g * NE + el2;
+                ow[k] = in ? el2 * ES + sLat[in ? a : 0] : -1;
+                const bool ok2 = in && e < nelem;
+                const size_t idx = ok2 ? (size_t)a * nelem + e : 0;
+                w[k][0] = (VISC == VISC_MU_E && ok2) ? ldg(mu_e + idx) : (real)0;
+                w[k][1] = ok2 ? ldg(mu_sgs + idx) : (real)0;
+            }
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                if (ov[k] < 0) continue;
+                dst[D_RHO * NPL + ov[k]] = v[k][0];
+                dst[D_T * NPL + ov[k]] = v[k][1];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) dst[(D_U0 + c) * NPL + ov[k]] = v[k][2 + c];
+                dst[D_MUF * NPL + ov[k]] = v[k][5];
+                if (VISC == VISC_MU_E) dst[D_MUE * NPL + ow[k]] = w[k][0];
+                dst[D_MUS * NPL + ow[k]] = w[k][1];
+            }
+            return;
+        }
         for (int i = tid; i < NE * N; i += NT) {
             const int el = i / N, l = i - el * N;
             const int I = l % Q, J = (l / Q) % Q, K = l / (Q * Q);
@@ -508,9 +608,9 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
 #pragma unroll
         for (int k = 0; k < MP; ++k) {
             const int i = tid + k * NT;
-            const int el = FUSEZ ? lt.el : i / N;
-            const int l = FUSEZ ? line_lat<2, Q>(lt.la, lt.lb, k) : i - el * N, e = g * NE + el;
-            const bool ok = (FUSEZ ? lt.active : i < NE * N) && e < nelem;
+            const int el = FUSEZ ? lt2.el : i / N;
+            const int l = FUSEZ ? line_lat<2, Q>(lt2.la, lt2.lb, k) : i - el * N, e = g * NE + el;
+            const bool ok = (FUSEZ ? lt2.active : i < NE * N) && e < nelem;
             const int a = ok ? sPerm[l] : 0;
             const real *hp = He + (ok ? ((size_t)e * N + a) * 9 : 0);
 #pragma unroll
@@ -527,8 +627,38 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                                    : sFs[D_MUE * NPL + o];
     };
 
+    // Staged He / gpvol: bulk copies of group g's spans (thread 0), the
+    // unaligned ends by plain loads (threads 32..37, 64..69).  Offsets of the
+    // spans' first words in the staging area.
+    int he_off = 0, gp_off = 0;
+    auto stage = [&](int g) {
+        if constexpr (STAGED) {
+            const int e0 = g * NE, e1 = min(e0 + NE, nelem);
+            const SpanPlan ph(He + (size_t)e0 * N * 9, (size_t)(e1 - e0) * N * 9 * sizeof(real));
+            const SpanPlan pg(gpvol + (size_t)e0 * N, (size_t)(e1 - e0) * N * sizeof(real));
+            if (tid == 0) {
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(sBar, ph.bulk + pg.bulk);
+                ph.issue(sHeB, sBar);
+                pg.issue(sGpB, sBar);
+            } else if (tid >= 32 && tid < 38) {
+                ph.plain(sHeB, tid - 32);
+            } else if (tid >= 64 && tid < 70) {
+                pg.plain(sGpB, tid - 64);
+            }
+            he_off = (int)(ph.shift / sizeof(real));
+            gp_off = (int)(pg.shift / sizeof(real));
+        }
+    };
+    unsigned phase = 0;
+
     int g = blockIdx.x;
     const int stride = gridDim.x;
+    if constexpr (STAGED) {
+        if (tid == 0) mbar_init(sBar, 1);
+        __syncthreads();
+        stage(g);
+    }
     int ids[IPT];
     load_ids(g, ids);
     __syncthreads();  // sLat ready
@@ -558,17 +688,26 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
         }
         run_net(g);
         if constexpr (FUSEZ) {
-            if (lt.active) {
-                grad_pass<G, 0>(lt, sFs, sX, sD);
-                grad_pass<G, 1>(lt, sFs, sX, sD);
+            if (lt0.active) grad_pass<G, 0>(lt0, sFs, sX, sD);
+            if (lt1.active) grad_pass<G, 1>(lt1, sFs, sX, sD);
+            if constexpr (STAGED) {
+                // Bounded wait for group g's spans; every thread learns the outcome.
+                const bool ok = mbar_wait(sBar, phase);
+                phase ^= 1u;
+                if (__syncthreads_or(!ok)) {
+                    if (tid == 0) report_wait_fault(tabs);
+                    return;
+                }
+            } else {
+                __syncthreads();
             }
-            __syncthreads();
             // Zeta stage, one thread per zeta line: the zeta derivatives at the
             // line's points (from its nodal values in registers), the point
             // pass there (the xi and eta fluxes are stored for their
             // divergence passes) and the zeta divergence of the zeta fluxes,
             // which stay in registers; the partial sums start the divergence.
-            if (lt.active) {
+            if (lt2.active) {
+                const LineThread<G> &lt = lt2;
                 constexpr int OST = Q * QP;
                 const int base = lt.el * ES + line_off<2, Q, QP>(lt.la, lt.lb, 0);
                 real v[5][Q];
@@ -588,10 +727,17 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                 // Late He rows: point c's row and gpvol, issued one point ahead.
                 auto he_row = [&](int c, real (&h)[9], real &gp) {
                     const int a = sPerm[line_lat<2, Q>(lt.la, lt.lb, c)];
-                    const real *hp = He + (eok ? ((size_t)ee * N + a) * 9 : 0);
+                    if constexpr (STAGED) {
+                        const real *hp = reinterpret_cast<const real *>(sHeB) + he_off + (lt.el * N + a) * 9;
 #pragma unroll
-                    for (int j = 0; j < 9; ++j) h[j] = eok ? ldg(hp + j) : (real)0;
-                    gp = eok ? ldg(gpvol + (size_t)ee * N + a) : (real)0;
+                        for (int j = 0; j < 9; ++j) h[j] = hp[j];
+                        gp = reinterpret_cast<const real *>(sGpB)[gp_off + lt.el * N + a];
+                    } else {
+                        const real *hp = He + (eok ? ((size_t)ee * N + a) * 9 : 0);
+#pragma unroll
+                        for (int j = 0; j < 9; ++j) h[j] = eok ? ldg(hp + j) : (real)0;
+                        gp = eok ? ldg(gpvol + (size_t)ee * N + a) : (real)0;
+                    }
                 };
                 real Hn[9], gpn;
                 if constexpr (LATE) he_row(0, Hn, gpn);
@@ -655,15 +801,16 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                 }
             }
             __syncthreads();
-            if (lt.active) div_pass<G, 0, false, false>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
-            __syncthreads();
-            if (lt.active) div_pass<G, 1, false, true>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
-        } else {
-            if (lt.active) {
-                grad_pass<G, 0>(lt, sFs, sX, sD);
-                grad_pass<G, 1>(lt, sFs, sX, sD);
-                grad_pass<G, 2>(lt, sFs, sX, sD);
+            if constexpr (STAGED) {
+                if (gn < ngroups) stage(gn);  // the spans of the next group, during the divergence
             }
+            if (lt0.active) div_pass<G, 0, false, false>(lt0, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            __syncthreads();
+            if (lt1.active) div_pass<G, 1, false, true>(lt1, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+        } else {
+            if (lt0.active) grad_pass<G, 0>(lt0, sFs, sX, sD);
+            if (lt1.active) grad_pass<G, 1>(lt1, sFs, sX, sD);
+            if (lt2.active) grad_pass<G, 2>(lt2, sFs, sX, sD);
             __syncthreads();
             // Point pass: physical gradients, stress and contravariant fluxes.
 #pragma unroll
@@ -691,11 +838,11 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                 sFs[P_KAP * NPL + o] = kappa_e(muf, me, ms, r, Cp, Pr);
             }
             __syncthreads();
-            if (lt.active) div_pass<G, 0, true, false>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            if (lt0.active) div_pass<G, 0, true, false>(lt0, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
             __syncthreads();
-            if (lt.active) div_pass<G, 1, false, false>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            if (lt1.active) div_pass<G, 1, false, false>(lt1, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
             __syncthreads();
-            if (lt.active) div_pass<G, 2, false, true>(lt, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            if (lt2.active) div_pass<G, 2, false, true>(lt2, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
         }
         __syncthreads();
         if (NBUF == 1 && gn < ngroups) {  // the next group's node ids, then its fields

@@ -17,13 +17,43 @@ constexpr int kTableNMax = (MSOD_MAX_PORDER + 1) * (MSOD_MAX_PORDER + 1) * (MSOD
 // Row pairs of the FP32 matrices for packed (f32x2) contractions:
 // Dp[((d*Q + c)*H + m)*2 + t] = D[d][2m+t][c] (zero for 2m+t = Q), H = (Q+1)/2.
 constexpr int kTableDPairMax = 3 * (MSOD_MAX_PORDER + 1) * (MSOD_MAX_PORDER + 2);
+// Even-odd form of the FP32 matrix (one direction), valid when the three
+// directions' matrices are equal and centro-antisymmetric, as the GLL
+// derivative matrix is: D[s'(r)][s'(c)] = -D[r][c] where s' mirrors a node
+// through the element centre.  Lines are stored in the reference's SOD 1-D
+// order (the two ends first, then the interior: natural indices 0, P, 1, ...,
+// P-1), where the mirror is sod_mirror.  With M = Q/2 mirror pairs (L_i,
+// s'(L_i)), L_i = sod_left(i), and for odd Q the centre node m:
+//   EO[i*M + j]           A = (D[L_i][L_j] - D[L_i][s'(L_j)]) / 2
+//   EO[M*M + i*M + j]     B = (D[L_i][L_j] + D[L_i][s'(L_j)]) / 2
+//   EO[2*M*M + i]         D[L_i][m]                         (odd Q)
+//   EO[2*M*M + M + j]     D[m][L_j]                         (odd Q)
+// so that, with e_j = v[L_j] + v[s'(L_j)] and o_j = v[L_j] - v[s'(L_j)],
+// d[L_i] = S_i + T_i and d[s'(L_i)] = S_i - T_i for S_i = sum_j A o_j and
+// T_i = sum_j B e_j (+ D[L_i][m] v[m]), and d[m] = sum_j D[m][L_j] o_j.
+__host__ __device__ constexpr int sod_mirror(int Q, int s) { return s == 0 ? 1 : (s == 1 ? 0 : Q + 1 - s); }
+__host__ __device__ constexpr int sod_left(int i) { return i == 0 ? 0 : i + 1; }
+__host__ __device__ constexpr int sod_centre(int Q) { return (Q + 1) / 2; }
+constexpr int kTableEOMax = 2 * (MSOD_MAX_PORDER / 2 + 1) * (MSOD_MAX_PORDER / 2 + 1) + 2 * (MSOD_MAX_PORDER / 2 + 1);
 struct TableScratch {
     float Df[kTableDMax];
+    float EO[kTableEOMax];
+    int eo_ok;  // 1 when EO represents all three directions' matrices
     double Dd[kTableDMax];
     alignas(8) float Dp[kTableDPairMax];
     int perm[kTableNMax];
     int lat[kTableNMax];
+    // Set (sticky, zero at allocation) by a kernel whose bounded wait for a
+    // bulk copy into shared memory ran out; the kernel then skipped its work.
+    // Checked mode reads and clears it after each call.
+    int wait_fault;
 };
+
+// Records a bounded wait that ran out (see TableScratch::wait_fault).
+__device__ __forceinline__ void report_wait_fault(const TableScratch *t)
+{
+    atomicOr(const_cast<int *>(&t->wait_fault), 1);
+}
 template <typename real>
 __host__ __device__ inline real *table_D(TableScratch *t);
 template <>
@@ -202,7 +232,8 @@ cudaError_t launch_features(int porder, const FeatureArgs &a, cudaStream_t st);
 cudaError_t launch_mlp_predict(int nelem, const float *feat, const __half *wh, const MlpNorm *nm, const float *numax,
                                float *y, float *nu, int *flag, cudaStream_t st);
 cudaError_t launch_mlp_norm(int n, const float *feat, MlpNorm *nm, cudaStream_t st);
-cudaError_t launch_mlp_grad(int n, const float *feat, const float *target, const int *idx, int batch, uint32_t seed,
+cudaError_t launch_mlp_grad(int n, const float *feat, const float *target, const float *weight, const int *idx,
+                            int batch, uint32_t seed,
                             int step, const float *master, const MlpNorm *nm, float *grad, float *loss, cudaStream_t st);
 cudaError_t launch_mlp_adam(float *master, float *m, float *v, float *grad, __half *wh, float lr, int t,
                             cudaStream_t st);

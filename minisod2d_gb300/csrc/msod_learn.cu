@@ -260,8 +260,8 @@ int msod_mlp_destroy(msod_mlp *m)
     return MSOD_OK;
 }
 
-int msod_mlp_train(msod_mlp *m, const float *feat, const float *target, int nsamples, int steps, int batch, float lr,
-                   uint64_t seed, float *loss_host, void *stream)
+int msod_mlp_train(msod_mlp *m, const float *feat, const float *target, const float *weight, int nsamples, int steps,
+                   int batch, float lr, uint64_t seed, float *loss_host, void *stream)
 {
     clear_error();
     if (!m || !feat || !target) return set_error(MSOD_ERR_INVALID_ARG, "NULL handle or training data");
@@ -275,7 +275,7 @@ int msod_mlp_train(msod_mlp *m, const float *feat, const float *target, int nsam
     if (!rc) rc = cuda_rc(cudaMemsetAsync(m->grad, 0, sizeof(float) * kMlpParams, st), "cudaMemsetAsync");
     if (!rc) rc = cuda_rc(launch_mlp_norm(nsamples, feat, m->norm, st), "normalisation launch");
     for (int t = 1; t <= steps && !rc; ++t) {
-        rc = cuda_rc(launch_mlp_grad(nsamples, feat, target, nullptr, batch, (uint32_t)seed, t, m->master, m->norm,
+        rc = cuda_rc(launch_mlp_grad(nsamples, feat, target, weight, nullptr, batch, (uint32_t)seed, t, m->master, m->norm,
                                      m->grad, loss + (t - 1), st),
                      "gradient launch");
         if (!rc) rc = cuda_rc(launch_mlp_adam(m->master, m->m, m->v, m->grad, m->wh, lr, t, st), "Adam launch");
@@ -288,8 +288,8 @@ int msod_mlp_train(msod_mlp *m, const float *feat, const float *target, int nsam
     return rc;
 }
 
-int msod_mlp_gradient(msod_mlp *m, const float *feat, const float *target, const int *idx, int batch,
-                      float *grad_host, void *stream)
+int msod_mlp_gradient(msod_mlp *m, const float *feat, const float *target, const float *weight, const int *idx,
+                      int batch, float *grad_host, void *stream)
 {
     clear_error();
     if (!m || !feat || !target || !idx || !grad_host || batch < 1)
@@ -297,7 +297,8 @@ int msod_mlp_gradient(msod_mlp *m, const float *feat, const float *target, const
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int rc = cuda_rc(cudaMemsetAsync(m->grad, 0, sizeof(float) * kMlpParams, st), "cudaMemsetAsync");
     if (!rc)
-        rc = cuda_rc(launch_mlp_grad(1, feat, target, idx, batch, 0u, 0, m->master, m->norm, m->grad, nullptr, st),
+        rc = cuda_rc(launch_mlp_grad(1, feat, target, weight, idx, batch, 0u, 0, m->master, m->norm, m->grad, nullptr,
+                                     st),
                      "gradient launch");
     if (!rc)
         rc = cuda_rc(cudaMemcpyAsync(grad_host, m->grad, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, st),

@@ -10,7 +10,8 @@
 //   network   12 -> 32 -> 32 -> 1, SiLU hidden units, softplus output,
 //             FP16 weights (FP32 master copy while training), FP32 accumulation
 //   training  mean-squared error of s against -log10 of the plain estimator's
-//             y (clamped to [1e-12, 1]) on feature -> y pairs, Adam (beta
+//             y (clamped to [1e-12, 1]) on feature -> y pairs, optionally
+//             weighted per sample (the caller's weights), Adam (beta
 //             0.9 / 0.999, eps 1e-8); the forward pass uses the FP16-rounded
 //             weights it will be deployed with
 //   fallback  an element whose features leave the training range [min, max]
@@ -350,10 +351,11 @@ __device__ __forceinline__ float warp_sum(float v)
 }
 
 // One batch: loss gradient accumulated into grad (sum over the batch of
-// dL/dparam with L = mean squared error).  Sample i of the batch is
-// idx ? idx[i] : hash(seed, step, i) mod n.
+// dL/dparam with L = the weighted mean squared error, weight[sample] or 1).
+// Sample i of the batch is idx ? idx[i] : hash(seed, step, i) mod n.
 __global__ void __launch_bounds__(256) mlp_grad_kernel(int n, const float *__restrict__ feat,
-                                                       const float *__restrict__ target, const int *__restrict__ idx,
+                                                       const float *__restrict__ target,
+                                                       const float *__restrict__ weight, const int *__restrict__ idx,
                                                        int batch, uint32_t seed, int step,
                                                        const float *__restrict__ master, const MlpNorm *__restrict__ nm,
                                                        float *__restrict__ grad, float *__restrict__ loss)
@@ -377,9 +379,10 @@ __global__ void __launch_bounds__(256) mlp_grad_kernel(int n, const float *__res
     Act s;
     mlp_forward(w, snm, x, s);
     const float t = live ? s_from_y(target[sidx]) : 0.0f;
-    const float dy = live ? 2.0f * (s.y - t) / (float)batch : 0.0f;
+    const float wt = live ? (weight ? weight[sidx] : 1.0f) : 0.0f;
+    const float dy = live ? 2.0f * wt * (s.y - t) / (float)batch : 0.0f;
     if (loss) {
-        const float l = warp_sum(live ? (s.y - t) * (s.y - t) / (float)batch : 0.0f);
+        const float l = warp_sum(live ? wt * (s.y - t) * (s.y - t) / (float)batch : 0.0f);
         if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
     }
     const float dz = dy * sigmoidf_(s.z);
@@ -466,10 +469,11 @@ cudaError_t launch_mlp_norm(int n, const float *feat, MlpNorm *nm, cudaStream_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_grad(int n, const float *feat, const float *target, const int *idx, int batch, uint32_t seed,
+cudaError_t launch_mlp_grad(int n, const float *feat, const float *target, const float *weight, const int *idx,
+                            int batch, uint32_t seed,
                             int step, const float *master, const MlpNorm *nm, float *grad, float *loss, cudaStream_t st)
 {
-    mlp_grad_kernel<<<(batch + 255) / 256, 256, 0, st>>>(n, feat, target, idx, batch, seed, step, master, nm, grad,
+    mlp_grad_kernel<<<(batch + 255) / 256, 256, 0, st>>>(n, feat, target, weight, idx, batch, seed, step, master, nm, grad,
                                                          loss);
     return cudaGetLastError();
 }

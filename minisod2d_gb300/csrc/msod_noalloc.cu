@@ -15,7 +15,9 @@
 // library and stays resident until the process exits.  Every call shares it
 // and it keeps the last call's value, so each call clears it first; calls that
 // overlap on the GPU (different streams, or different host threads on one
-// device) race on the word and must be serialised by the caller.
+// device) race on the word and must be serialised by the caller.  Every call
+// is synchronous (the verdict is copied back and the stream synchronised), so
+// no call may be made on a capturing stream or during a global-mode capture.
 #include <cuda_runtime.h>
 
 #include <mutex>

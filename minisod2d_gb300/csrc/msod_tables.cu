@@ -45,6 +45,33 @@ __global__ void table_prep_kernel(const int *__restrict__ invAtoIJK, const int *
         D[i] = dlxigp_ip[(size_t)(c * 3 + d) * N + sperm[l]];
     }
     if (sizeof(real) == 4) {
+        __syncthreads();  // D complete
+        // Even-odd form and its validity: the directions' matrices equal, the
+        // matrix centro-antisymmetric to within 1e-6 of its largest entry.
+        constexpr int M = Q / 2, mc = sod_centre(Q);
+        const float *Dv = out->Df;
+        for (int i = threadIdx.x; i < M * M; i += blockDim.x) {
+            const int r = sod_left(i / M), c = sod_left(i % M), cm = sod_mirror(Q, c);
+            out->EO[i] = 0.5f * (Dv[r * Q + c] - Dv[r * Q + cm]);
+            out->EO[M * M + i] = 0.5f * (Dv[r * Q + c] + Dv[r * Q + cm]);
+        }
+        if (Q % 2 == 1)
+            for (int i = threadIdx.x; i < M; i += blockDim.x) {
+                out->EO[2 * M * M + i] = Dv[sod_left(i) * Q + mc];
+                out->EO[2 * M * M + M + i] = Dv[mc * Q + sod_left(i)];
+            }
+        if (threadIdx.x == 0) {
+            float big = 0.0f;
+            for (int i = 0; i < Q * Q; ++i) big = fmaxf(big, fabsf(Dv[i]));
+            const float tol = 1e-6f * big;
+            bool ok = true;
+            for (int i = 0; i < Q * Q; ++i) {
+                const int r = i / Q, c = i % Q;
+                ok = ok && Dv[Q * Q + i] == Dv[i] && Dv[2 * Q * Q + i] == Dv[i];
+                ok = ok && fabsf(Dv[sod_mirror(Q, r) * Q + sod_mirror(Q, c)] + Dv[i]) <= tol;
+            }
+            out->eo_ok = ok ? 1 : 0;
+        }
         constexpr int H = (Q + 1) / 2;
         for (int i = threadIdx.x; i < 3 * Q * H * 2; i += blockDim.x) {
             const int t = i & 1, m = (i >> 1) % H, c = (i >> 1) / H % Q, d = (i >> 1) / (H * Q);

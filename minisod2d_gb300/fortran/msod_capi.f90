@@ -657,12 +657,13 @@ module msod_capi
          import :: c_int, c_ptr
          type(c_ptr), value :: m
       end function msod_mlp_destroy
-      integer(c_int) function msod_mlp_train(m, feat, target, nsamples, steps, batch, lr, seed, &
-            loss_host, stream) bind(C, name="msod_mlp_train")
+      integer(c_int) function msod_mlp_train(m, feat, target, weight, nsamples, steps, batch, lr, &
+            seed, loss_host, stream) bind(C, name="msod_mlp_train")
          import :: c_float, c_int, c_int64_t, c_ptr
          type(c_ptr), value :: m
          type(c_ptr), value :: feat
          type(c_ptr), value :: target
+         type(c_ptr), value :: weight
          integer(c_int), value :: nsamples
          integer(c_int), value :: steps
          integer(c_int), value :: batch
@@ -671,12 +672,13 @@ module msod_capi
          type(c_ptr), value :: loss_host
          type(c_ptr), value :: stream
       end function msod_mlp_train
-      integer(c_int) function msod_mlp_gradient(m, feat, target, idx, batch, grad_host, stream &
-            ) bind(C, name="msod_mlp_gradient")
+      integer(c_int) function msod_mlp_gradient(m, feat, target, weight, idx, batch, grad_host, &
+            stream) bind(C, name="msod_mlp_gradient")
          import :: c_int, c_ptr
          type(c_ptr), value :: m
          type(c_ptr), value :: feat
          type(c_ptr), value :: target
+         type(c_ptr), value :: weight
          type(c_ptr), value :: idx
          integer(c_int), value :: batch
          type(c_ptr), value :: grad_host

@@ -94,16 +94,16 @@ class Mlp:
         except Exception:
             pass
 
-    def train(self, feat, target, steps=2000, batch=4096, lr=1e-3, seed=0, stream=None):
+    def train(self, feat, target, steps=2000, batch=4096, lr=1e-3, seed=0, weight=None, stream=None):
         n = target.numel()
         loss = np.zeros(steps, np.float32)
-        capi.call("msod_mlp_train", self.h, _p(feat), _p(target), int(n), int(steps), int(batch), float(lr),
-                  int(seed), loss.ctypes.data_as(C.c_void_p), _stream(stream))
+        capi.call("msod_mlp_train", self.h, _p(feat), _p(target), _p(weight), int(n), int(steps), int(batch),
+                  float(lr), int(seed), loss.ctypes.data_as(C.c_void_p), _stream(stream))
         return loss
 
-    def gradient(self, feat, target, idx, stream=None):
+    def gradient(self, feat, target, idx, weight=None, stream=None):
         g = np.zeros(NPARAMS, np.float32)
-        capi.call("msod_mlp_gradient", self.h, _p(feat), _p(target), _p(idx), int(idx.numel()),
+        capi.call("msod_mlp_gradient", self.h, _p(feat), _p(target), _p(weight), _p(idx), int(idx.numel()),
                   g.ctypes.data_as(C.c_void_p), _stream(stream))
         return g
 

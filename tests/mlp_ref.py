@@ -70,13 +70,15 @@ def forward(w, norm, x):
     return y, (xh, a1, h1, a2, h2, z)
 
 
-def gradient(w, norm, x, t):
-    """d/dw of mean((s - s_from_y(t))^2) over the batch (flattened like the device layout)."""
+def gradient(w, norm, x, t, weight=None):
+    """d/dw of mean(weight (s - s_from_y(t))^2) over the batch (weight 1 if None; flattened like the
+    device layout)."""
     W1, b1, W2, b2, W3, b3 = unpack(w)
     y, (xh, a1, h1, a2, h2, z) = forward(w, norm, x)
     t = s_from_y(t)
     B = len(t)
-    dz = 2.0 * (y - t) / B * sig(z)
+    wt = np.ones(B) if weight is None else np.asarray(weight, np.float64)
+    dz = 2.0 * wt * (y - t) / B * sig(z)
     gW3 = dz @ h2
     gb3 = dz.sum()
     dh2 = dz[:, None] * W3[None, :]
@@ -97,9 +99,10 @@ def gradient(w, norm, x, t):
     return g
 
 
-def loss(w, norm, x, t):
+def loss(w, norm, x, t, weight=None):
     y, _ = forward(w, norm, x)
-    return float(np.mean((y - s_from_y(t)) ** 2))
+    wt = np.ones(len(t)) if weight is None else np.asarray(weight, np.float64)
+    return float(np.mean(wt * (y - s_from_y(t)) ** 2))
 
 
 def features(tables, geom, nelem, npoin, rho, u, pr, gamma=1.4, cmax=0.5):

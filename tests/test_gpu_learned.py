@@ -82,6 +82,14 @@ def test_gradient_matches_numpy(cuda):
     rel = np.linalg.norm(g - gr) / np.linalg.norm(gr)
     print("MLP gradient rel err %.2e" % rel)
     assert rel < 1e-4
+    # the per-sample weighted loss
+    wt = rng.uniform(0.1, 5.0, 300).astype(np.float32)
+    g = m.gradient(torch.from_numpy(x).to(cuda).reshape(-1), torch.from_numpy(t).to(cuda),
+                   torch.from_numpy(idx).to(cuda), weight=torch.from_numpy(wt).to(cuda))
+    gr = mlp_ref.gradient(mlp_ref.fp16_round(w), norm, x[idx], t[idx].astype(np.float64), wt[idx])
+    rel = np.linalg.norm(g - gr) / np.linalg.norm(gr)
+    print("MLP weighted gradient rel err %.2e" % rel)
+    assert rel < 1e-4
     # forward: prediction equals the numpy network on the FP16 weights
     y, _, flag = m.predict(torch.from_numpy(x).to(cuda).reshape(-1))
     yr, _ = mlp_ref.forward(mlp_ref.fp16_round(w), norm, x)

@@ -63,12 +63,13 @@ def test_numpy_mlp_gradient_finite_differences():
     norm = np.concatenate([rng.normal(0, 1, 12), rng.uniform(0.5, 2, 12), -np.ones(12) * 1e30, np.ones(12) * 1e30])
     x = rng.normal(0, 1, (16, 12))
     t = rng.uniform(0, 1, 16)
-    g = mlp_ref.gradient(w, norm, x, t)
-    for k in rng.choice(mlp_ref.NPARAMS, 40, replace=False):
-        e = np.zeros_like(w)
-        e[k] = 1e-6
-        fd = (mlp_ref.loss(w + e, norm, x, t) - mlp_ref.loss(w - e, norm, x, t)) / 2e-6
-        assert abs(fd - g[k]) <= 1e-6 + 1e-5 * abs(g[k])
+    for wt in (None, rng.uniform(0.1, 5.0, 16)):  # plain and per-sample weighted loss
+        g = mlp_ref.gradient(w, norm, x, t, wt)
+        for k in rng.choice(mlp_ref.NPARAMS, 40, replace=False):
+            e = np.zeros_like(w)
+            e[k] = 1e-6
+            fd = (mlp_ref.loss(w + e, norm, x, t, wt) - mlp_ref.loss(w - e, norm, x, t, wt)) / 2e-6
+            assert abs(fd - g[k]) <= 1e-6 + 1e-5 * abs(g[k])
 
 
 def test_numpy_features_are_finite():

@@ -7,6 +7,9 @@ msod_check_element_tables on the same inputs, call after call, and further calls
 must not change the device's free memory.
 """
 import ctypes as C
+import os
+import subprocess
+import sys
 
 import pytest
 
@@ -60,3 +63,47 @@ def test_noalloc_validation_matches_allocating_entry_point(cuda):
     a[1] = 1 << 30
     assert L.msod_check_element_tables_noalloc(*a) == capi.MSOD_ERR_INVALID_ARG
     assert b"int32" in L.msod_last_error_string()
+
+
+FRESH = r"""
+import ctypes as C, sys
+sys.path.insert(0, %r)
+from minisod2d_gb300 import capi, fem
+L = capi.lib()   # loaded before the context exists: with CUDA_MODULE_LOADING=EAGER its module loads with it
+import numpy as np, torch
+dev = torch.device("cuda:0")
+P = 4
+t = fem.element_tables(P)
+con, _, nelem, npoin = fem.structured_mesh(P, 3, 3, 3, t, 0.0, 0, coords=False)
+d = {k: torch.from_numpy(np.ascontiguousarray(t[k])).to(dev) for k in ("dlxigp_ip", "invAtoIJK", "AtoI", "AtoJ", "AtoK")}
+connec = torch.from_numpy(con).to(dev)
+args = [P, nelem, npoin] + [C.c_void_p(x.data_ptr()) for x in (connec, d["dlxigp_ip"], d["invAtoIJK"], d["AtoI"],
+                                                               d["AtoJ"], d["AtoK"])] + [None]
+torch.cuda.synchronize()
+free0 = torch.cuda.mem_get_info()[0]
+rcs = [L.msod_check_element_tables_noalloc(*args) for _ in range(5)]
+torch.cuda.synchronize()
+free1 = torch.cuda.mem_get_info()[0]
+rc_alloc = L.msod_check_element_tables(*args)   # the allocating entry point, as a control
+torch.cuda.synchronize()
+free2 = torch.cuda.mem_get_info()[0]
+print("RESULT", rcs, free0, free1, rc_alloc, free2)
+""" % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_noalloc_allocates_nothing_in_a_fresh_process(cuda):
+    """In a fresh process whose only library calls are the allocation-free entry point (inputs
+    built by torch, the library's module loaded eagerly with the context), five calls leave the
+    device's free memory unchanged."""
+    env = dict(os.environ, CUDA_MODULE_LOADING="EAGER")
+    out = subprocess.run([sys.executable, "-c", FRESH], capture_output=True, text=True, env=env, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = [x for x in out.stdout.splitlines() if x.startswith("RESULT")][-1]
+    rcs, rest = line[len("RESULT "):].split("]")
+    assert [int(x) for x in rcs.strip(" [").split(",")] == [capi.MSOD_OK] * 5
+    free0, free1, rc_alloc, free2 = (int(x) for x in rest.split())
+    assert free1 == free0
+    assert rc_alloc == capi.MSOD_OK
+    # The control: the allocating entry point's first call takes device memory where the
+    # measurement can see it (recorded, not required: the driver may sub-allocate).
+    print("control: the allocating entry point changed free memory by %d bytes" % (free1 - free2))
