@@ -98,8 +98,9 @@ DRIVER = os.path.join(HERE, "msod_driver")
 def build_driver():
     """The benchmark driver executable (main.f90 on the C ABI), linked to libmsod.so."""
     tmp = DRIVER + ".tmp"
-    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I" + INCLUDE, DRIVER_SRC, "-L" + HERE, "-lmsod",
-           "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I" + INCLUDE, "-I" + os.path.join(cuda, "include"), DRIVER_SRC,
+           "-L" + HERE, "-lmsod", "-L" + os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN", "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         print(" ".join(cmd))

@@ -533,6 +533,9 @@ __device__ __forceinline__ void convec_pass_x2(const float *__restrict__ sF, flo
 // line and field), 0 = the full matrix of direction 0.  Measured on plain_64
 // (unrolled passes, four blocks per SM): 1.48 ms against 1.62 ms for the
 // three full-matrix passes; porder 2 on 120^3 hexes 1.71 against 1.79 ms.
+// The contraction packed over pairs of fields (fma.rn.f32x2 on the even-odd
+// coefficients, no padding) measured slower, 1.51 ms at three blocks per SM
+// and 1.87 ms at four (its pairs of derivatives spill at 128 registers).
 #ifndef CONVEC_EO
 #define CONVEC_EO 1
 #endif

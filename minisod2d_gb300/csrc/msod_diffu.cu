@@ -67,6 +67,12 @@
 #ifndef DIFFU_LINEMAP
 #define DIFFU_LINEMAP 4
 #endif
+// The network of the learned viscosity (VISC_NET): 1 = evaluated for group
+// g+1 at the end of group g, while g+1's node fields are gathered (off the
+// critical path), 0 = evaluated for group g before its derivative passes.
+#ifndef DIFFU_NET_AHEAD
+#define DIFFU_NET_AHEAD 1
+#endif
 // Gather of the node fields: 0 = 4-byte cp.async copies, 1 = loads into
 // registers, then 32-lane shared-memory stores.  Measured: plain_64 1.466
 // against 1.483 ms (at three blocks per SM, DIFFU_MINB4=3), porder 5 on 64^3
@@ -414,6 +420,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     const int tid = threadIdx.x;
     const LineThread<G> lt0 = diffu_line<G>(tid, 0), lt1 = diffu_line<G>(tid, 1), lt2 = diffu_line<G>(tid, 2);
     constexpr bool FUSEZ = diffu_fusez<G>();
+    constexpr bool NET_AHEAD = VISC == VISC_NET && DIFFU_NET_AHEAD != 0 && DIFFU_NBUF == 1;
     constexpr bool LATE = FUSEZ && DIFFU_HE_LATE != 0;
     constexpr int MP = LATE ? 1 : (FUSEZ ? Q : IPT);  // points whose He and gpvol a thread holds
     for (int i = tid; i < N; i += NT) {
@@ -668,6 +675,12 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     load_net(g);
     int gn = g + stride;
     if (gn < ngroups) load_ids(gn, ids);
+    if constexpr (NET_AHEAD) {  // the first group's network now, the others' one group ahead
+        store_net();
+        __syncthreads();
+        run_net(g);
+        if (gn < ngroups) load_net(gn);
+    }
 
     int s = 0;
     for (; g < ngroups; g = gn, gn += stride, s = NBUF == 2 ? s ^ 1 : 0) {
@@ -676,7 +689,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
         real Hm[MP][9], gv[MP];
         if (!LATE) load_metric(g, Hm, gv);
         if (NBUF == 2 && gn < ngroups) store_ids(ids, sNode + (s ^ 1) * NPL);
-        store_net();
+        if (!NET_AHEAD) store_net();
         cp_async_wait_all();
         __syncthreads();
         if (gn < ngroups) {
@@ -684,9 +697,9 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                 gather(gn, sNode + (s ^ 1) * NPL, sF + (s ^ 1) * NDF * NPL);
                 if (gn + stride < ngroups) load_ids(gn + stride, ids);
             }
-            load_net(gn);
+            if (!NET_AHEAD) load_net(gn);
         }
-        run_net(g);
+        if (!NET_AHEAD) run_net(g);
         if constexpr (FUSEZ) {
             if (lt0.active) grad_pass<G, 0>(lt0, sFs, sX, sD);
             if (lt1.active) grad_pass<G, 1>(lt1, sFs, sX, sD);
@@ -850,6 +863,14 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
             __syncthreads();
             gather(gn, sNode, sF);
             if (gn + stride < ngroups) load_ids(gn + stride, ids);
+            if constexpr (NET_AHEAD) {
+                // The next group's network while its node fields are in flight
+                // (this group's viscosities were last read in its zeta stage).
+                store_net();
+                __syncthreads();
+                run_net(gn);
+                if (gn + stride < ngroups) load_net(gn + stride);
+            }
         }
     }
 }

@@ -9,13 +9,26 @@
 // run in timers.dat, the timing summary and the "Basic results" extrema on
 // stdout (:501-583) and, with --debug, results_convec.dat / results_diffu.dat
 // (:586-599).  Every call is timed as the reference times its synchronous
-// OpenACC regions: wall clock around the call and a stream synchronisation.
-// A JSON summary (results.json) adds the throughput of the hex pair.
+// OpenACC regions: wall clock around the call and a stream synchronisation;
+// CUDA events recorded on the stream around the same call time it on the
+// device (timers_events.dat, same columns and format).  A JSON summary
+// (results.json) adds both averages and the throughput of the hex pair.
 //
 //   msod_driver [--porder 4] [--nelem 192000] [--nruns 100]
 //               [--mesh disconnected|structured --nx N --jitter J]
 //               [--fields reference|smooth|shock --seed S] [--device D]
+//               [--precision fp32|fp16|bf16] [--mu-e given|plain|learned]
+//               [--weights FILE] [--fp64-check]
 //               [--out DIR] [--debug] [--format-check]
+//
+// --precision and --mu-e choose the form of the two hex calls through
+// msod_set_mode: the FP32 kernels or the FP16 / BF16 tensor-core kernels, and
+// the caller's mu_e, the plain entropy-viscosity estimator or the learned one
+// (the network in --weights, with the estimator as per-element fallback).
+// --fp64-check then runs the FP64 build of the hex calls on the same inputs
+// promoted to FP64 (with the plain estimator's mu_e when the viscosity is
+// estimated) and prints and records the relative L2 distance of every
+// residual.
 //
 // Defaults are the reference's compile-time parameters (mod_constants.f90:16,
 // main.f90:21-22).  The tet kernels use npoin_t = 4 floor(npoin/4) nodes (the
@@ -30,6 +43,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "msod.h"
 
 namespace {
@@ -39,7 +54,8 @@ struct Options {
     double jitter = 0.0;
     uint64_t seed = 0;
     std::string mesh = "disconnected", fields = "reference", out = ".";
-    bool debug = false, format_check = false;
+    std::string precision = "fp32", mu_e = "given", weights;
+    bool debug = false, format_check = false, fp64_check = false;
 };
 
 [[noreturn]] void die(const char *what, int rc)
@@ -120,6 +136,10 @@ Options parse(int argc, char **argv)
         else if (a == "--seed") o.seed = std::strtoull(val("--seed"), nullptr, 10);
         else if (a == "--device") o.device = std::atoi(val("--device"));
         else if (a == "--out") o.out = val("--out");
+        else if (a == "--precision") o.precision = val("--precision");
+        else if (a == "--mu-e") o.mu_e = val("--mu-e");
+        else if (a == "--weights") o.weights = val("--weights");
+        else if (a == "--fp64-check") o.fp64_check = true;
         else if (a == "--debug") o.debug = true;
         else if (a == "--format-check") o.format_check = true;
         else {
@@ -129,11 +149,39 @@ Options parse(int argc, char **argv)
     }
     if (o.porder < 1 || o.porder > MSOD_MAX_PORDER || o.nruns < 1 || o.nelem < 1 || o.nx < 1 ||
         (o.mesh != "disconnected" && o.mesh != "structured") ||
-        (o.fields != "reference" && o.fields != "smooth" && o.fields != "shock")) {
+        (o.fields != "reference" && o.fields != "smooth" && o.fields != "shock") ||
+        (o.precision != "fp32" && o.precision != "fp16" && o.precision != "bf16") ||
+        (o.mu_e != "given" && o.mu_e != "plain" && o.mu_e != "learned") || (o.mu_e == "learned" && o.weights.empty())) {
         std::fprintf(stderr, "msod_driver: bad option value\n");
         std::exit(2);
     }
     return o;
+}
+
+void cuda_check(cudaError_t err, const char *what)
+{
+    if (err != cudaSuccess) {
+        std::fprintf(stderr, "msod_driver: %s failed: %s\n", what, cudaGetErrorString(err));
+        std::exit(1);
+    }
+}
+
+// Relative L2 distance of an FP32 result from its FP64 reference.
+double rel_l2(const std::vector<float> &a, const std::vector<double> &b)
+{
+    double num = 0.0, den = 0.0;
+    for (size_t i = 0; i < a.size(); ++i) {
+        const double d = (double)a[i] - b[i];
+        num += d * d;
+        den += b[i] * b[i];
+    }
+    return den > 0.0 ? std::sqrt(num / den) : std::sqrt(num);
+}
+
+template <typename T>
+std::vector<double> widen(const std::vector<T> &v)
+{
+    return std::vector<double>(v.begin(), v.end());
 }
 
 // Device copy of a host array.
@@ -154,10 +202,11 @@ T *device_array(size_t n)
     return static_cast<T *>(d);
 }
 
-std::vector<float> download(const float *d, size_t n)
+template <typename T = float>
+std::vector<T> download(const T *d, size_t n)
 {
-    std::vector<float> h(n);
-    check(msod_d2h(h.data(), d, n * sizeof(float), nullptr), "msod_d2h");
+    std::vector<T> h(n);
+    check(msod_d2h(h.data(), d, n * sizeof(T), nullptr), "msod_d2h");
     check(msod_stream_synchronize(nullptr), "msod_stream_synchronize");
     return h;
 }
@@ -285,6 +334,16 @@ int main(int argc, char **argv)
     const std::vector<float> ones_t(4 * (size_t)nelem_t, 1.0f);
     float *d_mue_t = upload(ones_t), *d_mus_t = upload(ones_t);
 
+    // The form of the two hex calls (msod_set_mode).
+    const int prec = o.precision == "fp16" ? MSOD_PREC_FP16 : (o.precision == "bf16" ? MSOD_PREC_BF16 : MSOD_PREC_FP32);
+    const int mue_mode = o.mu_e == "plain" ? MSOD_MU_E_PLAIN : (o.mu_e == "learned" ? MSOD_MU_E_LEARNED : MSOD_MU_E_GIVEN);
+    msod_mlp *mlp = nullptr;
+    if (mue_mode == MSOD_MU_E_LEARNED) {
+        check(msod_mlp_create(&mlp, 0), "msod_mlp_create");
+        check(msod_mlp_load(mlp, o.weights.c_str()), "msod_mlp_load");
+    }
+    check(msod_set_mode(prec, mue_mode, mlp), "msod_set_mode");
+
     // Residual arrays.
     auto res = [&](size_t m) { return device_array<float>(m); };
     float *Rm = res(np), *Rq = res(3 * np), *Re = res(np), *Rms = res(np), *Rqs = res(3 * np), *Res = res(np);
@@ -293,11 +352,23 @@ int main(int argc, char **argv)
     float *Dmt = res(npoin_t), *Dqt = res(3 * (size_t)npoin_t), *Det = res(npoin_t);
     const float Cp = 1.0f, Pra = 1.0f;  // main.f90:412-413
 
-    auto timed = [](auto &&call) {
+    // Wall clock around the call and a stream synchronisation (the reference's
+    // MPI_Wtime pair around a synchronous region), and CUDA events recorded on
+    // the stream around the same call (device time, seconds, in *ev).
+    cudaEvent_t ev0, ev1;
+    cuda_check(cudaEventCreate(&ev0), "cudaEventCreate");
+    cuda_check(cudaEventCreate(&ev1), "cudaEventCreate");
+    auto timed = [&](double *ev, auto &&call) {
         const auto t0 = std::chrono::steady_clock::now();
+        cuda_check(cudaEventRecord(ev0, nullptr), "cudaEventRecord");
         call();
+        cuda_check(cudaEventRecord(ev1, nullptr), "cudaEventRecord");
         check(msod_stream_synchronize(nullptr), "msod_stream_synchronize");
-        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        float ms = 0.0f;
+        cuda_check(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
+        *ev = 1e-3 * (double)ms;
+        return wall;
     };
 
     const std::string timers_path = o.out + "/timers.dat";
@@ -306,30 +377,37 @@ int main(int argc, char **argv)
         std::fprintf(stderr, "msod_driver: cannot open %s: %s\n", timers_path.c_str(), std::strerror(errno));
         return 1;
     }
-    Stats sc, ss, st, sd, sdt;
+    const std::string events_path = o.out + "/timers_events.dat";
+    FILE *ef = std::fopen(events_path.c_str(), "w");
+    if (!ef) {
+        std::fprintf(stderr, "msod_driver: cannot open %s: %s\n", events_path.c_str(), std::strerror(errno));
+        return 1;
+    }
+    Stats sc, ss, st, sd, sdt, ec, es, et, ed, edt;
     for (int i = 1; i <= o.nruns; ++i) {
-        const double tc = timed([&] {
+        double xc, xs, xt, xd, xdt;
+        const double tc = timed(&xc, [&] {
             check(msod_convec_ijk(P, nelem, npoin, d_connec, nullptr, nullptr, d_He, d_gpvol, d_dlx, nullptr, d_inv,
                                   d_AI, d_AJ, d_AK, d_u, d_q, d_rho, d_pr, d_E, Rm, Rq, Re, nullptr),
                   "msod_convec_ijk");
         });
-        const double ts = timed([&] {
+        const double ts = timed(&xs, [&] {
             check(msod_convec_ijk_split(P, nelem, npoin, d_connec, nullptr, nullptr, d_He, d_gpvol, d_dlx, nullptr,
                                         d_inv, d_AI, d_AJ, d_AK, d_u, d_q, d_rho, d_pr, d_E, Rms, Rqs, Res, nullptr),
                   "msod_convec_ijk_split");
         });
-        const double tt = timed([&] {
+        const double tt = timed(&xt, [&] {
             check(msod_fem_convec(nelem_t, npoin_t, d_connec_t, d_tN, d_tdN, d_He_t, d_gpvol_t, d_u, d_q, d_rho,
                                   d_pr, d_E, Rmt, Rqt, Ret, nullptr),
                   "msod_fem_convec");
         });
-        const double td = timed([&] {
+        const double td = timed(&xd, [&] {
             check(msod_diffusion_ijk(P, nelem, npoin, d_connec, nullptr, nullptr, d_He, d_gpvol, d_dlx, nullptr,
                                      d_inv, d_AI, d_AJ, d_AK, Cp, Pra, d_rho, d_u, d_Tem, d_muf, d_mue, d_mus, Dm,
                                      Dq, De, nullptr),
                   "msod_diffusion_ijk");
         });
-        const double tdt = timed([&] {
+        const double tdt = timed(&xdt, [&] {
             check(msod_fem_diffu(nelem_t, npoin_t, d_connec_t, d_tN, d_tdN, d_He_t, d_gpvol_t, Cp, Pra, d_rho, d_u,
                                  d_Tem, d_muf, d_mue_t, d_mus_t, Dmt, Dqt, Det, nullptr),
                   "msod_fem_diffu");
@@ -339,10 +417,20 @@ int main(int argc, char **argv)
         st.add(tt);
         sd.add(td);
         sdt.add(tdt);
+        ec.add(xc);
+        es.add(xs);
+        et.add(xt);
+        ed.add(xd);
+        edt.add(xdt);
         const double row[4] = {tc, tt, td, tdt};
         std::fprintf(tf, "%s\n", timers_line(i, row).c_str());
+        const double erow[4] = {xc, xt, xd, xdt};
+        std::fprintf(ef, "%s\n", timers_line(i, erow).c_str());
     }
     std::fclose(tf);
+    std::fclose(ef);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
 
     // Timing summary (main.f90:501-537).
     const double nr = (double)o.nruns;
@@ -407,6 +495,59 @@ int main(int argc, char **argv)
         }
     }
 
+    // FP64 check: the FP64 build of the hex calls on the same inputs promoted to
+    // FP64 (mu_e: the caller's, or the plain estimator's when it is estimated).
+    double fe[6] = {0, 0, 0, 0, 0, 0};
+    if (o.fp64_check) {
+        auto up64 = [&](const std::vector<double> &h) { return upload(h); };
+        const std::vector<double> He64 = widen(download(d_He, 9 * ne)), gp64 = widen(download(d_gpvol, ne));
+        double *e_He = up64(He64), *e_gp = up64(gp64), *e_dlx = up64(widen(dlx));
+        double *e_u = up64(widen(u)), *e_q = up64(widen(q)), *e_rho = up64(widen(rho)), *e_pr = up64(widen(pr));
+        double *e_E = up64(widen(E)), *e_Tem = up64(widen(Tem)), *e_muf = up64(widen(muf)), *e_mus = up64(widen(mus));
+        std::vector<double> mue64;
+        if (mue_mode == MSOD_MU_E_GIVEN) {
+            mue64 = widen(mue);
+        } else {
+            // The plain estimator on the pressure the estimated modes use, p = rho Rgas Tem
+            // (main.f90:52: Rgas = 287, gamma = 1.4; ce = 0.1, cmax = 0.5).
+            std::vector<float> ph(np);
+            for (size_t i = 0; i < np; ++i) ph[i] = rho[i] * 287.0f * Tem[i];
+            float *d_p = upload(ph), *mu_p = device_array<float>(ne);
+            check(msod_entropy_viscosity(P, nelem, npoin, d_connec, d_He, d_gpvol, d_dlx, d_inv, d_AI, d_AJ, d_AK, d_rho,
+                                         d_u, d_p, 1.4f, 0.1f, 0.5f, 1, mu_p, nullptr, nullptr, nullptr),
+                  "msod_entropy_viscosity");
+            mue64 = widen(download(mu_p, ne));
+            msod_free(mu_p);
+            msod_free(d_p);
+        }
+        double *e_mue = up64(mue64);
+        double *c_m = device_array<double>(np), *c_q = device_array<double>(3 * np), *c_e = device_array<double>(np);
+        double *f_m = device_array<double>(np), *f_q = device_array<double>(3 * np), *f_e = device_array<double>(np);
+        check(msod_convec_ijk_f64(P, nelem, npoin, d_connec, e_He, e_gp, e_dlx, d_inv, d_AI, d_AJ, d_AK, e_u, e_q,
+                                  e_rho, e_pr, e_E, c_m, c_q, c_e, nullptr),
+              "msod_convec_ijk_f64");
+        check(msod_diffusion_ijk_f64(P, nelem, npoin, d_connec, e_He, e_gp, e_dlx, d_inv, d_AI, d_AJ, d_AK, 1.0, 1.0,
+                                     e_rho, e_u, e_Tem, e_muf, e_mue, e_mus, f_m, f_q, f_e, nullptr),
+              "msod_diffusion_ijk_f64");
+        fe[0] = rel_l2(hRm, download(c_m, np));
+        fe[1] = rel_l2(hRq, download(c_q, 3 * np));
+        fe[2] = rel_l2(hRe, download(c_e, np));
+        fe[3] = rel_l2(hDm, download(f_m, np));
+        fe[4] = rel_l2(hDq, download(f_q, 3 * np));
+        fe[5] = rel_l2(hDe, download(f_e, np));
+        for (void *ptr : {(void *)e_He, (void *)e_gp, (void *)e_dlx, (void *)e_u, (void *)e_q, (void *)e_rho,
+                          (void *)e_pr, (void *)e_E, (void *)e_Tem, (void *)e_muf, (void *)e_mus, (void *)e_mue,
+                          (void *)c_m, (void *)c_q, (void *)c_e, (void *)f_m, (void *)f_q, (void *)f_e})
+            msod_free(ptr);
+        std::printf(" FP64 check (%s, mu_e %s; relative L2 against the FP64 build on the same inputs):\n",
+                    o.precision.c_str(), o.mu_e.c_str());
+        std::printf(" Convec Rmass %s Rmom %s Rener %s\n", fortran_e(fe[0], 4).c_str(), fortran_e(fe[1], 4).c_str(),
+                    fortran_e(fe[2], 4).c_str());
+        std::printf(" Diffu  Dmass %s Dmom %s Dener %s\n", fortran_e(fe[3], 4).c_str(), fortran_e(fe[4], 4).c_str(),
+                    fortran_e(fe[5], 4).c_str());
+        std::printf(" ----------------------------------------\n");
+    }
+
     // JSON summary.
     const std::string jpath = o.out + "/results.json";
     if (FILE *j = std::fopen(jpath.c_str(), "w")) {
@@ -415,11 +556,30 @@ int main(int argc, char **argv)
                      "\"mesh\": \"%s\", \"fields\": \"%s\", \"nruns\": %d, "
                      "\"avg_s\": {\"convec\": %.9e, \"convec_split\": %.9e, \"convec_tet\": %.9e, "
                      "\"diffu\": %.9e, \"diffu_tet\": %.9e}, "
-                     "\"hex_gdofs\": %.6f, \"timing\": \"wall clock around each call and a stream synchronisation\"}\n",
+                     "\"avg_event_s\": {\"convec\": %.9e, \"convec_split\": %.9e, \"convec_tet\": %.9e, "
+                     "\"diffu\": %.9e, \"diffu_tet\": %.9e}, "
+                     "\"hex_gdofs\": %.6f, \"hex_gdofs_event\": %.6f, \"precision\": \"%s\", \"mu_e\": \"%s\", "
+                     "\"fp64_check\": %s, "
+                     "\"timing\": \"avg_s: wall clock around each call and a stream synchronisation; avg_event_s: CUDA "
+                     "events on the stream around the same call\"}\n",
                      P, nelem, npoin, nelem_t, npoin_t, o.mesh.c_str(), o.fields.c_str(), o.nruns, ac, as, at, ad, adt,
-                     5.0 * npoin / (ac + ad) / 1e9);
+                     ec.sum / nr, es.sum / nr, et.sum / nr, ed.sum / nr, edt.sum / nr, 5.0 * npoin / (ac + ad) / 1e9,
+                     5.0 * npoin / ((ec.sum + ed.sum) / nr) / 1e9, o.precision.c_str(), o.mu_e.c_str(),
+                     o.fp64_check ? "true" : "false");
         std::fclose(j);
     }
+    if (o.fp64_check) {
+        const std::string fpath = o.out + "/fp64_check.json";
+        if (FILE *j = std::fopen(fpath.c_str(), "w")) {
+            std::fprintf(j,
+                         "{\"precision\": \"%s\", \"mu_e\": \"%s\", \"Rmass\": %.6e, \"Rmom\": %.6e, "
+                         "\"Rener\": %.6e, \"Dmass\": %.6e, \"Dmom\": %.6e, \"Dener\": %.6e}\n",
+                         o.precision.c_str(), o.mu_e.c_str(), fe[0], fe[1], fe[2], fe[3], fe[4], fe[5]);
+            std::fclose(j);
+        }
+    }
+    msod_set_mode(MSOD_PREC_FP32, MSOD_MU_E_GIVEN, nullptr);
+    if (mlp) msod_mlp_destroy(mlp);
     msod_finalize();
     return 0;
 }

@@ -174,11 +174,29 @@ def diffusion_ijk_nu(dev, nu, out=None, stream=None):
     return out
 
 
-def training_data(cfg, seeds, device="cuda"):
-    """Features and targets y = nu / nu_max of the plain estimator over seeded field instances."""
+def loss_weights(y, numax, feat, share):
+    """Per-sample weights of the training loss (mean 1): a uniform part 1 - share and a part
+    `share` proportional to (nu * J)^2, nu = y nu_max the plain estimator's viscosity and J the
+    element's relative density jump (feature 0 is its logarithm).  The artificial mass
+    diffusion nu_e div grad rho (elem_diffu.f90:183) is set almost entirely by the few shock
+    elements with the largest nu J; a decade error there costs Rmass in proportion to nu J, while
+    the uniform part keeps the fit of every decade."""
     import torch
 
-    feats, ys = [], []
+    if share <= 0.0:
+        return None
+    jump = torch.exp(feat.view(-1, NFEAT)[:, 0].double())
+    m = (y.double() * numax.double() * jump) ** 2
+    m = m / torch.clamp(m.mean(), min=1e-300)
+    return ((1.0 - share) + share * m).float().contiguous()
+
+
+def training_data(cfg, seeds, device="cuda", with_numax=False):
+    """Features and targets y = nu / nu_max of the plain estimator over seeded field instances
+    (and nu_max with ``with_numax``)."""
+    import torch
+
+    feats, ys, nms = [], [], []
     host = dev = None
     for s in seeds:
         if host is None:
@@ -192,6 +210,9 @@ def training_data(cfg, seeds, device="cuda"):
         f, _ = features(dev)
         ys.append(torch.clamp(nu / torch.clamp(numax, min=1e-30), 0.0, 1.0))
         feats.append(f.clone())
+        nms.append(numax.clone())
+    if with_numax:
+        return torch.cat(feats), torch.cat(ys), torch.cat(nms)
     return torch.cat(feats), torch.cat(ys)
 
 
@@ -242,24 +263,28 @@ def evaluate(mlp, dev, ybar=None, reps=5):
     # first-order bound nu_max everywhere, and nu_max times the mean training ratio.
     out_b = [torch.empty_like(x) for x in out_p]
     diffusion_ijk_nu(dev, numax, out_b)
-    r = {
-        "nu_rel_l2": rel(nu_l, nu_p),
-        "mu_e_rel_l2": rel(_mu_from_nu(dev, nu_l), mu_p),
-        "Rmass_rel_l2": rel(out_l[0], out_p[0]),
-        "Rmom_rel_l2": rel(out_l[1], out_p[1]),
-        "Rener_rel_l2": rel(out_l[2], out_p[2]),
-        "fallback_fraction": float(flag.float().mean()),
-        "numax_everywhere": {"nu_rel_l2": rel(numax, nu_p), "Rmom_rel_l2": rel(out_b[1], out_p[1]),
-                             "Rener_rel_l2": rel(out_b[2], out_p[2])},
-    }
+    def errs(nu_x, out_x):
+        return {"nu_rel_l2": rel(nu_x, nu_p), "Rmass_rel_l2": rel(out_x[0], out_p[0]),
+                "Rmom_rel_l2": rel(out_x[1], out_p[1]), "Rener_rel_l2": rel(out_x[2], out_p[2])}
+
+    r = dict(errs(nu_l, out_l))
+    r["mu_e_rel_l2"] = rel(_mu_from_nu(dev, nu_l), mu_p)
+    r["fallback_fraction"] = float(flag.float().mean())
+    r["numax_everywhere"] = errs(numax, out_b)
     if ybar is not None:
         nu_c = float(ybar) * numax
         diffusion_ijk_nu(dev, nu_c, out_b)
-        r["constant_ratio"] = {"nu_rel_l2": rel(nu_c, nu_p), "Rmom_rel_l2": rel(out_b[1], out_p[1]),
-                               "Rener_rel_l2": rel(out_b[2], out_p[2])}
+        r["constant_ratio"] = errs(nu_c, out_b)
+    # The constant fraction of nu_max closest to the plain estimator in the Rmass sense: Rmass is
+    # linear in nu, so the best c minimises |c R1 - Rp| with R1 the mass residual of nu_max.
+    diffusion_ijk_nu(dev, numax, out_b)
+    R1, Rp = out_b[0].double(), out_p[0].double()
+    c_best = float(torch.dot(R1, Rp) / torch.clamp(torch.dot(R1, R1), min=1e-300))
+    nu_c = c_best * numax
+    diffusion_ijk_nu(dev, nu_c, out_b)
+    r["best_constant_for_Rmass"] = dict(errs(nu_c, out_b), fraction=c_best)
     diffusion_ijk_nu(dev, torch.zeros_like(numax), out_b)
-    r["no_artificial_viscosity"] = {"nu_rel_l2": 1.0, "Rmom_rel_l2": rel(out_b[1], out_p[1]),
-                                    "Rener_rel_l2": rel(out_b[2], out_p[2])}
+    r["no_artificial_viscosity"] = errs(torch.zeros_like(numax), out_b)
     mu_buf, nu_buf, nm_buf = torch.empty_like(mu_p), torch.empty_like(nu_p), torch.empty_like(numax)
     nu_lb, flag_b = torch.empty_like(nu_l), torch.empty_like(flag)
 
@@ -281,25 +306,98 @@ def evaluate(mlp, dev, ybar=None, reps=5):
     return r
 
 
+# Feature 0 is log(relative density jump + 1e-12); norm = mean[12], inv_std[12], fmin[12], fmax[12].
+_FMAX0 = 3 * NFEAT
+
+
+def set_trusted_jump(mlp, log_jump_max):
+    """Cap the trusted range of feature 0 (the element's relative density jump): elements above
+    it take the plain estimator's viscosity (the per-element fallback of both learned paths)."""
+    _, norm = mlp.params()
+    norm = norm.copy()
+    norm[_FMAX0] = min(float(norm[_FMAX0]), float(log_jump_max))
+    mlp.set_params(None, norm)
+
+
+def rmass_error(mlp, dev):
+    """Relative L2 of the artificial mass diffusion with the learned viscosity (fallback
+    included) against the plain estimator, and the fallback fraction."""
+    import torch
+
+    _, nu_p, _ = entropy_viscosity(dev)
+    out_p = [torch.empty_like(x) for x in (dev.Dmass, dev.Dmom, dev.Dener)]
+    diffusion_ijk_nu(dev, nu_p, out_p)
+    nu_l, flag = learned_viscosity(mlp, dev)
+    out_l = [torch.empty_like(x) for x in out_p]
+    diffusion_ijk_nu(dev, nu_l, out_l)
+    d = float(torch.linalg.vector_norm((out_l[0] - out_p[0]).double()))
+    return d / max(float(torch.linalg.vector_norm(out_p[0].double())), 1e-300), float(flag.float().mean())
+
+
+def choose_shock_band(mlp, cfg, feat0, val_seeds, target, fractions=(0.002, 0.005, 0.01, 0.02, 0.03, 0.05, 0.08,
+                                                                     0.12, 0.2), device="cuda"):
+    """The shock band: the smallest share of elements, by relative density jump (the training
+    elements' feature 0 quantiles), whose fallback to the plain estimator brings the artificial
+    mass diffusion within ``target`` (relative L2, mean over the validation seeds).  Sets the
+    trusted range on the network and returns (log jump threshold, share, validation errors)."""
+    import torch
+
+    _, norm0 = mlp.params()
+    host = dev = None
+    devs = []
+    for s in val_seeds:
+        c = workload.Config(cfg.name, cfg.porder, cfg.nx, cfg.jitter, cfg.kind, cfg.nmodes, int(s))
+        host = workload.HostCase(c) if host is None else host.with_seed(int(s))
+        devs.append(host)
+    dev = workload.DeviceCase(devs[0], device=device)
+    f0 = feat0.double()
+    tried = []
+    for frac in sorted(fractions):
+        thr = float(torch.quantile(f0[torch.randperm(f0.numel(), device=f0.device)[:1 << 22]], 1.0 - frac))
+        mlp.set_params(None, norm0)
+        set_trusted_jump(mlp, thr)
+        errs = []
+        for h in devs:
+            dev.set_fields(h)
+            errs.append(rmass_error(mlp, dev))
+        e = float(np.mean([x[0] for x in errs]))
+        tried.append({"share": frac, "log_jump_max": thr, "val_Rmass_rel_l2": e,
+                      "val_fallback": float(np.mean([x[1] for x in errs]))})
+        if e <= target:
+            return thr, frac, tried
+    return thr, frac, tried
+
+
 def train_and_evaluate(cfg, train_seeds, eval_seeds, steps=2000, batch=4096, lr=1e-3, seed=0, weights=None,
-                       device="cuda"):
+                       device="cuda", shock_share=0.0, band_target=None, val_seeds=()):
     """Train the network on the plain estimator's output over ``train_seeds``
     and evaluate it on ``eval_seeds`` (the same mesh, other field instances).
-    Returns a report dict; writes the weight file if ``weights`` is given."""
+    ``shock_share`` > 0 weights the loss towards the shock elements
+    (``loss_weights``).  Returns a report dict; writes the weight file if
+    ``weights`` is given."""
     import time
 
     import torch
 
     t0 = time.time()
-    feat, y = training_data(cfg, train_seeds, device=device)
+    feat, y, nmx = training_data(cfg, train_seeds, device=device, with_numax=True)
+    wt = loss_weights(y, nmx, feat, shock_share)
+    del nmx
     t_data = time.time() - t0
     mlp = Mlp(seed=seed)
     t0 = time.time()
-    loss = mlp.train(feat, y, steps=steps, batch=batch, lr=lr, seed=seed)
+    loss = mlp.train(feat, y, steps=steps, batch=batch, lr=lr, seed=seed, weight=wt)
     t_train = time.time() - t0
     ybar = float(y.double().mean())
-    del feat, y
+    feat0 = feat.view(-1, NFEAT)[:, 0].clone()
+    del feat, y, wt
     torch.cuda.empty_cache()
+    band = None
+    if band_target is not None:
+        thr, share, tried = choose_shock_band(mlp, cfg, feat0, val_seeds, band_target, device=device)
+        band = {"target_Rmass_rel_l2": band_target, "val_seeds": [int(s) for s in val_seeds], "log_jump_max": thr,
+                "share_of_training_elements": share, "tried": tried}
+    del feat0
     if weights:
         mlp.save(weights)
     host = workload.HostCase(workload.Config(cfg.name, cfg.porder, cfg.nx, cfg.jitter, cfg.kind, cfg.nmodes,
@@ -320,14 +418,15 @@ def train_and_evaluate(cfg, train_seeds, eval_seeds, steps=2000, batch=4096, lr=
             "ms_plain_estimator", "ms_learned_estimator", "ms_plain_estimator_plus_diffusion",
             "ms_learned_estimator_plus_diffusion")
     summary = {k: mean(k) for k in keys}
-    for sub in ("numax_everywhere", "constant_ratio", "no_artificial_viscosity"):
+    for sub in ("numax_everywhere", "constant_ratio", "best_constant_for_Rmass", "no_artificial_viscosity"):
         summary[sub] = {k: mean(k, sub) for k in per_seed[0][sub]}
     summary["time_saved_fraction"] = 1.0 - summary["ms_learned_estimator_plus_diffusion"] / \
         summary["ms_plain_estimator_plus_diffusion"]
     return {
         "workload": cfg.name, "porder": cfg.porder, "nelem": cfg.nelem, "npoin": cfg.npoin,
         "train_seeds": [int(s) for s in train_seeds], "eval_seeds": [int(s) for s in eval_seeds],
-        "steps": steps, "batch": batch, "lr": lr, "samples": int(len(train_seeds) * cfg.nelem), "ybar": ybar,
+        "steps": steps, "batch": batch, "lr": lr, "shock_share": shock_share, "shock_band": band,
+        "samples": int(len(train_seeds) * cfg.nelem), "ybar": ybar,
         "loss_first_50": float(loss[:50].mean()), "loss_last_50": float(loss[-50:].mean()),
         "seconds_data": t_data, "seconds_train": t_train,
         "mean": summary, "per_seed": per_seed,
@@ -345,6 +444,11 @@ def _main(argv=None):
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--shock-share", type=float, default=0.0,
+                    help="share of the loss weight on the shock elements (see loss_weights)")
+    ap.add_argument("--band-target", type=float, default=None,
+                    help="Rmass relative L2 the shock-band fallback must reach on the validation seeds")
+    ap.add_argument("--nval", type=int, default=2, help="validation seeds (500, 501, ...) for the shock band")
     ap.add_argument("--weights", default=None, help="weight file to write (default data/mlp_<config>.bin)")
     ap.add_argument("--report", default=None, help="report to write (default data/<config>_report.json)")
     a = ap.parse_args(argv)
@@ -353,7 +457,8 @@ def _main(argv=None):
     a.report = a.report or os.path.join(DATA, "%s_report.json" % a.config)
     train = list(range(a.ntrain))
     ev = list(range(1000, 1000 + a.neval))
-    rep = train_and_evaluate(cfg, train, ev, a.steps, a.batch, a.lr, weights=a.weights)
+    rep = train_and_evaluate(cfg, train, ev, a.steps, a.batch, a.lr, weights=a.weights, shock_share=a.shock_share,
+                             band_target=a.band_target, val_seeds=list(range(500, 500 + a.nval)))
     txt = json.dumps(rep, indent=1)
     if a.report:
         with open(a.report, "w") as f:

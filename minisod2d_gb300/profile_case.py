@@ -10,6 +10,7 @@ convec_mixed, diffu_mixed (``--precision`` fp16 / bf16), estimator (plain
 entropy viscosity), learned (features + network + fallback, with a freshly
 initialised network unless ``--weights`` names a weight file), diffu_learned
 (the diffusion with the network in its prologue; needs ``--weights``),
+diffu_nu (the diffusion with one viscosity per element),
 tet_convec / tet_diffu (fem_convec / fem_diffu on the reference driver's
 disconnected tetrahedra over the case's nodes).
 """
@@ -69,6 +70,11 @@ def main(argv=None):
                 calls.append(lambda: learn.learned_viscosity(mlp, dev))
             else:
                 calls.append(lambda: learn.diffusion_learned(mlp, dev))
+        elif k == "diffu_nu":
+            import torch as _t
+
+            nu_c = _t.full((dev.nelem,), 1e-3, device=dev.rho.device)
+            calls.append(lambda: learn.diffusion_ijk_nu(dev, nu_c))
         else:
             raise SystemExit("unknown kernel %r" % k)
     for fn in calls:

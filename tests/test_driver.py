@@ -120,3 +120,38 @@ def test_driver_structured_mesh_matches_the_oracle(cuda, tmp_path):
         got = (a[:, 1], np.concatenate([a[:, 2], a[:, 3], a[:, 4]]), a[:, 5])
         for g, r64 in zip(got, ref):
             assert R.rel_l2(g, r64) < 2e-5, name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,mu_e,conv_bound,diff_bound", [
+    ("fp32", "given", 1e-5, 1e-4), ("fp16", "given", 2e-4, 5e-3), ("bf16", "given", 1e-3, 2e-2),
+    ("fp32", "plain", 1e-5, 1e-4), ("fp32", "learned", 1e-5, 1.0), ("fp16", "learned", 2e-4, 1.0)])
+def test_driver_modes(cuda, tmp_path, precision, mu_e, conv_bound, diff_bound):
+    """The driver's switches (main.f90's timing loop with the precision and viscosity forms of
+    msod_set_mode): every mode runs, keeps the timers.dat format, times each call with CUDA events
+    beside the wall clock, and its FP64 check (the FP64 build on the same inputs; for an estimated
+    viscosity, with the plain estimator's mu_e) stays within the mode's accuracy."""
+    from minisod2d_gb300 import learn
+
+    nruns = 2
+    args = [_driver(), "--porder", "4", "--mesh", "structured", "--nx", "6", "--jitter", "0.05", "--fields", "shock",
+            "--seed", "3", "--nruns", str(nruns), "--precision", precision, "--mu-e", mu_e, "--fp64-check",
+            "--out", str(tmp_path)]
+    if mu_e == "learned":
+        args += ["--weights", learn.shipped_weights("learned_48")]
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "Avg. convective time" in r.stdout and "FP64 check" in r.stdout
+    pat = re.compile(r"^[ \d]{3}( [ \d.]{15}\d){4} $")
+    for name in ("timers.dat", "timers_events.dat"):
+        rows = (tmp_path / name).read_text().splitlines()
+        assert len(rows) == nruns and all(pat.match(row) for row in rows), (name, rows)
+    s = json.loads((tmp_path / "results.json").read_text())
+    assert s["precision"] == precision and s["mu_e"] == mu_e and s["fp64_check"] is True
+    assert all(v > 0 for v in s["avg_event_s"].values())
+    assert all(s["avg_event_s"][k] <= s["avg_s"][k] * 1.5 + 1e-4 for k in s["avg_s"])
+    f = json.loads((tmp_path / "fp64_check.json").read_text())
+    print("DRIVER %s %s %s" % (precision, mu_e, {k: "%.2e" % v for k, v in f.items() if k not in ("precision", "mu_e")}))
+    assert max(f["Rmass"], f["Rmom"], f["Rener"]) < conv_bound
+    assert max(f["Dmom"], f["Dener"]) < min(diff_bound, 0.1)
+    assert f["Dmass"] < diff_bound

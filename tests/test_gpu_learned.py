@@ -191,25 +191,48 @@ def test_network_gains_over_estimators_without_entropy_residual(cuda):
     assert m["fallback_fraction"] < 0.5
 
 
-def test_shipped_network_on_held_out_learned_48_seed(cuda):
-    """The committed network (trained on 64 seeds of the 48^3 shock workload)
-    on a seed it never saw: close to the plain estimator, far closer than the
-    best constant fraction of nu_max, few fallbacks."""
-    cfg = workload.CONFIGS["learned_48"]
+def _shipped_on_held_out(cuda, name):
+    import json
+
+    cfg = workload.CONFIGS[name]
     host = workload.HostCase(workload.Config(cfg.name, cfg.porder, cfg.nx, cfg.jitter, cfg.kind, cfg.nmodes, 2024))
     dev = workload.DeviceCase(host, device=cuda)
     m = learn.Mlp()
-    m.load(learn.SHIPPED_WEIGHTS)
-    import json
-
-    rep = json.load(open(os.path.join(os.path.dirname(learn.SHIPPED_WEIGHTS), "learned_48_report.json")))
+    m.load(learn.shipped_weights(name))
+    rep = json.load(open(os.path.join(os.path.dirname(learn.SHIPPED_WEIGHTS), "%s_report.json" % name)))
     r = learn.evaluate(m, dev, ybar=rep["ybar"], reps=1)
-    print("SHIPPED nu err %.3e const %.3e Rmom %.2e Rener %.2e fallback %.2e" % (
-        r["nu_rel_l2"], r["constant_ratio"]["nu_rel_l2"], r["Rmom_rel_l2"], r["Rener_rel_l2"], r["fallback_fraction"]))
-    assert r["nu_rel_l2"] < 0.4
+    print("SHIPPED %s nu err %.3e (const %.3e) Rmass %.3e (const %.3e, best const %.3e) Rmom %.2e Rener %.2e "
+          "fallback %.3f" % (name, r["nu_rel_l2"], r["constant_ratio"]["nu_rel_l2"], r["Rmass_rel_l2"],
+                             r["constant_ratio"]["Rmass_rel_l2"], r["best_constant_for_Rmass"]["Rmass_rel_l2"],
+                             r["Rmom_rel_l2"], r["Rener_rel_l2"], r["fallback_fraction"]))
+    return r
+
+
+def _check_shipped(r):
+    # The artificial mass diffusion nu_e div grad rho (elem_diffu.f90:183) is set by the few
+    # shock elements with the largest viscosity: the shock band takes the plain estimator's
+    # value (per-element fallback), the network the rest.
+    assert r["Rmass_rel_l2"] <= 0.1
+    assert r["Rmass_rel_l2"] < 0.5 * r["constant_ratio"]["Rmass_rel_l2"]
+    assert r["Rmass_rel_l2"] < 0.5 * r["best_constant_for_Rmass"]["Rmass_rel_l2"]
     assert r["nu_rel_l2"] < 0.5 * r["constant_ratio"]["nu_rel_l2"]
-    assert r["Rmom_rel_l2"] < 0.01 and r["Rener_rel_l2"] < 0.02
-    assert r["fallback_fraction"] < 0.01
+    assert r["Rmom_rel_l2"] < 0.01 and r["Rener_rel_l2"] < 0.01
+    assert r["fallback_fraction"] < 0.15
+
+
+def test_shipped_network_on_held_out_learned_48_seed(cuda):
+    """The committed network (trained on 64 seeds of the 48^3 shock workload, shock band chosen
+    on two validation seeds) on a seed it never saw: the artificial mass diffusion within 0.1 of
+    the plain estimator's, far closer than any constant fraction of nu_max."""
+    r = _shipped_on_held_out(cuda, "learned_48")
+    _check_shipped(r)
+    assert r["nu_rel_l2"] < 0.4
+
+
+def test_shipped_network_on_held_out_combined_96_seed(cuda):
+    """The same for the combined workload's network (96^3 hexes, porder 5, 16 training seeds)."""
+    r = _shipped_on_held_out(cuda, "combined_96")
+    _check_shipped(r)
 
 
 def _learned_from_T(m, dev):
