@@ -79,6 +79,10 @@ d = {k: torch.from_numpy(np.ascontiguousarray(t[k])).to(dev) for k in ("dlxigp_i
 connec = torch.from_numpy(con).to(dev)
 args = [P, nelem, npoin] + [C.c_void_p(x.data_ptr()) for x in (connec, d["dlxigp_ip"], d["invAtoIJK"], d["AtoI"],
                                                                d["AtoJ"], d["AtoK"])] + [None]
+# One kernel launch and one device-to-host copy before the measured window: the driver sets up
+# per-context state at the first launch (8 MiB on this GPU, the size of the default device-side
+# malloc heap), which belongs to no library call.
+warm = torch.ones(4, device=dev).add_(1.0).sum().item()
 torch.cuda.synchronize()
 free0 = torch.cuda.mem_get_info()[0]
 rcs = [L.msod_check_element_tables_noalloc(*args) for _ in range(5)]
@@ -93,8 +97,9 @@ print("RESULT", rcs, free0, free1, rc_alloc, free2)
 
 def test_noalloc_allocates_nothing_in_a_fresh_process(cuda):
     """In a fresh process whose only library calls are the allocation-free entry point (inputs
-    built by torch, the library's module loaded eagerly with the context), five calls leave the
-    device's free memory unchanged."""
+    built by torch, the library's module loaded eagerly with the context, the context's first
+    kernel launch done by torch beforehand), five calls leave the device's free memory
+    unchanged."""
     env = dict(os.environ, CUDA_MODULE_LOADING="EAGER")
     out = subprocess.run([sys.executable, "-c", FRESH], capture_output=True, text=True, env=env, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
