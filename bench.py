@@ -515,7 +515,6 @@ def variant_learned(reps):
     r["workload"] = "learned_48: 48^3 hexes, porder 4, shock-like fields, held-out seed 2024"
     r["speedup_estimator_plus_diffusion"] = r["ms_plain_estimator_plus_diffusion"] / \
         r["ms_learned_estimator_plus_diffusion"]
-    r["speedup_fused"] = r["ms_plain_estimator_plus_diffusion"] / r["ms_fused_learned_diffusion"]
     return r
 
 
@@ -548,11 +547,6 @@ def variant_combined(reps):
 
     def learned32():
         dev.convec()
-        learn.learned_viscosity(m, dev, nu_l, flag)
-        learn.diffusion_ijk_nu(dev, nu_l)
-
-    def learned_fused():
-        dev.convec()
         learn.diffusion_learned(m, dev, nu=nu_l, flag=flag)
 
     def mixed_learned():
@@ -560,15 +554,12 @@ def variant_combined(reps):
         learn.learned_viscosity(m, dev, nu_l, flag)
         dev.diffu_mixed("fp16", nu_elem=nu_l, out=o64b)
 
-    t_plain, t_l32, t_lf, t_ml = _ms(plain, reps), _ms(learned32, reps), _ms(learned_fused, reps), \
-        _ms(mixed_learned, reps)
+    t_plain, t_l32, t_ml = _ms(plain, reps), _ms(learned32, reps), _ms(mixed_learned, reps)
     plain()
     pe = {"convec": {k: _rel(a, b) for k, a, b in zip(names, (dev.Rmass, dev.Rmom, dev.Rener), c64)},
           "diffu": {k: _rel(a, b) for k, a, b in zip(names, (dev.Dmass, dev.Dmom, dev.Dener), d64)}}
     learned32()
     le = {"diffu": {k: _rel(a, b) for k, a, b in zip(names, (dev.Dmass, dev.Dmom, dev.Dener), d64)}}
-    learned_fused()
-    lfe = {"diffu": {k: _rel(a, b) for k, a, b in zip(names, (dev.Dmass, dev.Dmom, dev.Dener), d64)}}
     mixed_learned()
     me = {"convec": {k: _rel(a, b) for k, a, b in zip(names, o64, c64)},
           "diffu": {k: _rel(a, b) for k, a, b in zip(names, o64b, d64)}}
@@ -578,10 +569,9 @@ def variant_combined(reps):
             "error_reference": "FP64 build of the plain kernels on the same inputs, diffusion with the plain "
                                "estimator's mu_e",
             "plain": {"ms": t_plain, "gdofs": dofs / t_plain / 1e6, "err": pe},
-            "learned_fp32": {"ms": t_l32, "gdofs": dofs / t_l32 / 1e6, "err": le, "speedup": t_plain / t_l32},
-            "learned_fp32_fused": {"ms": t_lf, "gdofs": dofs / t_lf / 1e6, "err": lfe, "speedup": t_plain / t_lf,
-                                   "path": "convection + msod_diffusion_ijk_learned (network in the diffusion "
-                                           "prologue)"},
+            "learned_fp32": {"ms": t_l32, "gdofs": dofs / t_l32 / 1e6, "err": le, "speedup": t_plain / t_l32,
+                             "path": "convection + msod_diffusion_ijk_learned (features kernel with the network, "
+                                     "fallback estimator on the flagged elements, per-element-viscosity diffusion)"},
             "mixed_fp16_learned": {"ms": t_ml, "gdofs": dofs / t_ml / 1e6, "err": me, "speedup": t_plain / t_ml},
             "fallback_fraction": float(flag.float().mean()),
             "nu_rel_l2_learned_vs_plain": _rel(nu_l, nu_p)}

@@ -392,8 +392,10 @@ int msod_mlp_predict(const msod_mlp *m, const float *feat, const float *numax_el
 /* Weight file with a CRC-32; a failed check returns MSOD_ERR_BAD_MODEL. */
 int msod_mlp_save(const msod_mlp *m, const char *path);
 int msod_mlp_load(msod_mlp *m, const char *path);
-/* nu per element from the network; elements flagged out of range take the
- * plain estimator's value. */
+/* nu per element from the network (evaluated inside the features kernel,
+ * one warp per element, with the bits of msod_mlp_predict); elements flagged
+ * out of range take the plain estimator's value (computed for those
+ * elements only). */
 int msod_learned_viscosity(const msod_mlp *m, int porder, int nelem, int npoin, const int *connec,
                            const float *He, const float *gpvol, const float *dlxigp_ip,
                            const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
@@ -401,12 +403,12 @@ int msod_learned_viscosity(const msod_mlp *m, int porder, int nelem, int npoin, 
                            float Rgas, float gamma, float ce, float cmax, float *nu_elem, int *flag,
                            void *stream);
 /* No counterpart in the reference: full_diffusion_ijk with the artificial
- * viscosity from the network, evaluated per element in the diffusion
- * kernel's prologue.  The features take the pressure p_or_T (Rgas = 0) or
- * p = rho Rgas T from the temperature p_or_T (Rgas > 0).  Elements whose
- * features leave the network's training range take the plain estimator's
- * value (computed for those elements only).  nu_elem and flag (nelem each,
- * optional) receive the viscosity used and the fallback flags. */
+ * viscosity from the network -- msod_learned_viscosity followed by
+ * msod_diffusion_ijk_nu on the same stream.  The features take the pressure
+ * p_or_T (Rgas = 0) or p = rho Rgas T from the temperature p_or_T (Rgas > 0).
+ * Elements whose features leave the network's training range take the plain
+ * estimator's value (computed for those elements only).  nu_elem and flag
+ * (nelem each, optional) receive the viscosity used and the fallback flags. */
 int msod_diffusion_ijk_learned(const msod_mlp *m, int porder, int nelem, int npoin, const int *connec,
                                const float *He, const float *gpvol, const float *dlxigp_ip,
                                const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,

@@ -183,12 +183,12 @@ static int diffu_impl(int porder, int nelem, int npoin, const int *connec, const
                       const real *dlx, const int *inv, const int *ai, const int *aj, const int *ak, real Cp, real Pr,
                       const real *rho, const real *u, const real *Tem, const real *mu_fluid, const real *mu_e,
                       const real *mu_sgs, real *Rmass, real *Rmom, real *Rener, void *stream,
-                      const real *nu_elem = nullptr, const DiffuNet *net = nullptr)
+                      const real *nu_elem = nullptr)
 {
     clear_error();
     int rc = check_geometry(porder, nelem, npoin, connec, He, gpvol, dlx, inv, ai, aj, ak);
     if (rc) return rc;
-    if (!rho || !u || !Tem || !mu_fluid || !(mu_e || nu_elem || net) || !mu_sgs || !Rmass || !Rmom || !Rener)
+    if (!rho || !u || !Tem || !mu_fluid || !(mu_e || nu_elem) || !mu_sgs || !Rmass || !Rmom || !Rener)
         return set_error(MSOD_ERR_INVALID_ARG, "NULL field or residual array");
     if (!(Pr != (real)0)) return set_error(MSOD_ERR_INVALID_ARG, "Pr must be non-zero");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -204,7 +204,6 @@ static int diffu_impl(int porder, int nelem, int npoin, const int *connec, const
     a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlx;
     a.invAtoIJK = inv; a.AtoI = ai; a.AtoJ = aj; a.AtoK = ak; a.Cp = Cp; a.Pr = Pr;
     a.rho = rho; a.u = u; a.Tem = Tem; a.mu_fluid = mu_fluid; a.mu_e = mu_e; a.mu_sgs = mu_sgs; a.nu_elem = nu_elem;
-    if (net) a.net = *net;
     a.Rmass = Rmass; a.Rmom = Rmom; a.Rener = Rener;
     rc = cuda_status(launch_table_prep<real>(porder, a, tabs, st), "table preparation launch");
     if (!rc) rc = cuda_status(launch_diffu_plain<real>(porder, a, tabs, st), "diffusion kernel launch");
@@ -346,23 +345,6 @@ int msod_diffusion_ijk_nu(int porder, int nelem, int npoin, const int *connec, c
                              gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, nullptr, mu_sgs, Rmass, Rmom, Rener, stream,
                              nu_elem);
 }
-
-}  // extern "C"
-
-namespace msod {
-int diffusion_with_net(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
-                       const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
-                       const int *gmshAtoK, float Cp, float Pr, const float *rho, const float *u, const float *Tem,
-                       const float *mu_fluid, const float *mu_sgs, const DiffuNet &net, float *Rmass, float *Rmom,
-                       float *Rener, void *stream)
-{
-    return diffu_impl<float>(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
-                             gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, nullptr, mu_sgs, Rmass, Rmom, Rener, stream,
-                             nullptr, &net);
-}
-}  // namespace msod
-
-extern "C" {
 
 int msod_convec_ijk_f64(int porder, int nelem, int npoin, const int *connec, const double *He, const double *gpvol,
                         const double *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,

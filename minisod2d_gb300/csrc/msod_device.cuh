@@ -304,6 +304,18 @@ struct SpanPlan {
     }
 };
 
+// Appends e to list[*count ..] for every lane whose f is set, with one atomic
+// per warp; every lane of the warp calls it (the list order is unspecified).
+__device__ __forceinline__ void warp_append(bool f, int e, int *list, int *count)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (m && lane == __ffs(m) - 1) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, m ? __ffs(m) - 1 : 0);
+    if (f) list[base + __popc(m & ((1u << lane) - 1u))] = e;
+}
+
 // Grid of a persistent kernel: resident blocks per SM x SMs, capped by the work.
 template <typename Kernel>
 inline int persistent_grid(Kernel kern, int threads, size_t smem, int ngroups)

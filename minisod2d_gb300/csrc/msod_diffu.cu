@@ -43,7 +43,6 @@
 
 #include "msod_device.cuh"
 #include "msod_kernels.h"
-#include "msod_mlp.cuh"
 
 // Zeta stage (one thread per line only): 1 = the zeta derivatives, the point
 // pass and the zeta divergence run as one pass over each zeta line, with the
@@ -66,12 +65,6 @@
 // 1.503 ms; porder 5 on 64^3 hexes 2.99 against 2.96 ms (off there).
 #ifndef DIFFU_LINEMAP
 #define DIFFU_LINEMAP 4
-#endif
-// The network of the learned viscosity (VISC_NET): 1 = evaluated for group
-// g+1 at the end of group g, while g+1's node fields are gathered (off the
-// critical path), 0 = evaluated for group g before its derivative passes.
-#ifndef DIFFU_NET_AHEAD
-#define DIFFU_NET_AHEAD 1
 #endif
 // Gather of the node fields: 0 = 4-byte cp.async copies, 1 = loads into
 // registers, then 32-lane shared-memory stores.  Measured: plain_64 1.466
@@ -371,21 +364,9 @@ constexpr int diffu_necap()
 template <typename real, int P>
 using DiffuGeom = LineGeom<real, P, diffu_necap<real, P>(), diffu_s<real, P>()>;
 
-// Viscosity source of the diffusion kernel.
-enum { VISC_MU_E = 0, VISC_NU_ELEM = 1, VISC_NET = 2 };
-
-// Shared memory of the network mode: transposed weights (lane j of a warp
-// reads unit j of each input: conflict-free), the group's features and
-// per-element inputs, and the viscosity per element.
-constexpr int kNetW1T = 0, kNetB1 = kNetW1T + kMlpIn * kMlpH, kNetW2T = kNetB1 + kMlpH,
-              kNetB2 = kNetW2T + kMlpH * kMlpH, kNetW3 = kNetB2 + kMlpH, kNetB3 = kNetW3 + kMlpH,
-              kNetWords = kNetB3 + 1;
-
-template <class G>
-constexpr size_t net_smem_floats()
-{
-    return (size_t)kNetWords + G::NE * (kMlpIn + 4);
-}
+// Viscosity source of the diffusion kernel: the mu_e array, or one value per
+// element (mu_e(e, a) = rho(a) nu_elem(e)).
+enum { VISC_MU_E = 0, VISC_NU_ELEM = 1 };
 
 template <class G, int VISC>
 __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
@@ -396,7 +377,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                  const typename G::real *__restrict__ Tem, const typename G::real *__restrict__ mu_fluid,
                  const typename G::real *__restrict__ mu_e, const typename G::real *__restrict__ mu_sgs,
                  const typename G::real *__restrict__ nu_elem, typename G::real *__restrict__ Rmass,
-                 typename G::real *__restrict__ Rmom, typename G::real *__restrict__ Rener, DiffuNet net)
+                 typename G::real *__restrict__ Rmom, typename G::real *__restrict__ Rener)
 {
     using real = typename G::real;
     constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT, NPL = G::NPL;
@@ -413,14 +394,10 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);  // [NBUF][NPL]
     int *sPerm = sNode + NBUF * NPL;
     int *sLat = sPerm + N;
-    float *sNet = reinterpret_cast<float *>(sLat + N);  // network mode: weights, then per-group data
-    float *sFeat = sNet + kNetWords;                      // [NE][12]
-    float *sInfo = sFeat + NE * kMlpIn;                   // [NE][4]: numax, flag, fallback nu, nu
 
     const int tid = threadIdx.x;
     const LineThread<G> lt0 = diffu_line<G>(tid, 0), lt1 = diffu_line<G>(tid, 1), lt2 = diffu_line<G>(tid, 2);
     constexpr bool FUSEZ = diffu_fusez<G>();
-    constexpr bool NET_AHEAD = VISC == VISC_NET && DIFFU_NET_AHEAD != 0 && DIFFU_NBUF == 1;
     constexpr bool LATE = FUSEZ && DIFFU_HE_LATE != 0;
     constexpr int MP = LATE ? 1 : (FUSEZ ? Q : IPT);  // points whose He and gpvol a thread holds
     for (int i = tid; i < N; i += NT) {
@@ -429,103 +406,6 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     }
     if (G::S > 1)
         for (int i = tid; i < 3 * Q * Q; i += NT) sD[i] = table_D<real>(tabs)[i];
-    if (VISC == VISC_NET) {
-        for (int i = tid; i < kMlpParams; i += NT) {
-            const float w = __half2float(net.wh[i]);
-            int d;
-            if (i < kOffB1) d = kNetW1T + (i % kMlpIn) * kMlpH + i / kMlpIn;          // W1[j][k] -> [k][j]
-            else if (i < kOffW2) d = kNetB1 + (i - kOffB1);
-            else if (i < kOffB2) d = kNetW2T + ((i - kOffW2) % kMlpH) * kMlpH + (i - kOffW2) / kMlpH;
-            else if (i < kOffW3) d = kNetB2 + (i - kOffB2);
-            else if (i < kOffB3) d = kNetW3 + (i - kOffW3);
-            else d = kNetB3;
-            sNet[d] = w;
-        }
-    }
-    // Network mode: the group's features and per-element inputs, loaded one
-    // group ahead into registers (thread t < 12 NE: one feature; t < NE also
-    // numax, flag, fallback nu).
-    float pf_feat = 0.0f, pf_numax = 0.0f, pf_flag = 0.0f, pf_fb = 0.0f;
-    auto load_net = [&](int g) {
-        if (VISC != VISC_NET) return;
-        if (tid < NE * kMlpIn) {
-            const int e = g * NE + tid / kMlpIn;
-            pf_feat = e < nelem ? ldg(net.feat + (size_t)e * kMlpIn + tid % kMlpIn) : 0.0f;
-        }
-        if (tid < NE) {
-            const int e = g * NE + tid;
-            const bool ok = e < nelem;
-            pf_numax = ok ? ldg(net.numax + e) : 0.0f;
-            pf_flag = ok ? (float)ldg(net.flag + e) : 0.0f;
-            pf_fb = (ok && pf_flag != 0.0f) ? ldg(net.nu_fb + e) : 0.0f;
-        }
-    };
-    auto store_net = [&]() {
-        if (VISC != VISC_NET) return;
-        if (tid < NE * kMlpIn) {  // normalised here, as the prediction kernel does
-            const int k = tid % kMlpIn;
-            sFeat[tid] = (pf_feat - ldg(&net.norm->mean[k])) * ldg(&net.norm->inv_std[k]);
-        }
-        if (tid < NE) {
-            sInfo[tid * 4 + 0] = pf_numax;
-            sInfo[tid * 4 + 1] = pf_flag;
-            sInfo[tid * 4 + 2] = pf_fb;
-        }
-    };
-    // One warp per element (a warp interleaves its elements): the network in
-    // the operation order of the prediction kernel, or the plain estimator's
-    // value for flagged elements.
-    auto run_net = [&](int g) {
-        if (VISC != VISC_NET) return;
-        constexpr int NW = NT / 32, ELW = (NE + NW - 1) / NW;
-        const int lane = tid & 31, warp = tid >> 5;
-        float a1[ELW], h1[ELW], a2[ELW], z[ELW];
-#pragma unroll
-        for (int q = 0; q < ELW; ++q) a1[q] = sNet[kNetB1 + lane];
-#pragma unroll
-        for (int k = 0; k < kMlpIn; ++k) {
-            const float w = sNet[kNetW1T + k * kMlpH + lane];
-#pragma unroll
-            for (int q = 0; q < ELW; ++q) {
-                const int el = min(warp + q * NW, NE - 1);
-                a1[q] = fmaf(w, sFeat[el * kMlpIn + k], a1[q]);
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < ELW; ++q) {
-            h1[q] = silu(a1[q]);
-            a2[q] = sNet[kNetB2 + lane];
-        }
-#pragma unroll
-        for (int k = 0; k < kMlpH; ++k) {
-            const float w = sNet[kNetW2T + k * kMlpH + lane];
-#pragma unroll
-            for (int q = 0; q < ELW; ++q) a2[q] = fmaf(w, __shfl_sync(0xffffffffu, h1[q], k), a2[q]);
-        }
-#pragma unroll
-        for (int q = 0; q < ELW; ++q) {
-            h1[q] = silu(a2[q]);  // the second hidden layer's outputs
-            z[q] = sNet[kNetB3];
-        }
-#pragma unroll
-        for (int j = 0; j < kMlpH; ++j) {
-            const float w = sNet[kNetW3 + j];
-#pragma unroll
-            for (int q = 0; q < ELW; ++q) z[q] = fmaf(w, __shfl_sync(0xffffffffu, h1[q], j), z[q]);
-        }
-#pragma unroll
-        for (int q = 0; q < ELW; ++q) {
-            const int el = warp + q * NW, e = g * NE + el;
-            if (el >= NE) continue;
-            float nu = 0.0f;
-            if (e < nelem) {
-                nu = sInfo[el * 4 + 1] != 0.0f ? sInfo[el * 4 + 2] : y_from_s(softplus(z[q])) * sInfo[el * 4 + 0];
-                if (lane == 0 && net.nu_out) net.nu_out[e] = nu;
-            }
-            if (lane == 0) sInfo[el * 4 + 3] = nu;
-        }
-    };
-
     auto load_ids = [&](int g, int (&ids)[IPT]) {
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
@@ -629,9 +509,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     // mu_e at a point of element el of group g (lattice offset o, density r).
     auto point_mu_e = [&](int g, int el, int o, real r, const real *sFs) -> real {
         const int ee = g * NE + el;
-        return VISC == VISC_NU_ELEM ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0)
-               : VISC == VISC_NET  ? r * (real)sInfo[el * 4 + 3]
-                                   : sFs[D_MUE * NPL + o];
+        return VISC == VISC_NU_ELEM ? (ee < nelem ? r * ldg(nu_elem + ee) : (real)0) : sFs[D_MUE * NPL + o];
     };
 
     // Staged He / gpvol: bulk copies of group g's spans (thread 0), the
@@ -672,15 +550,8 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     store_ids(ids, sNode);
     __syncthreads();
     gather(g, sNode, sF);
-    load_net(g);
     int gn = g + stride;
     if (gn < ngroups) load_ids(gn, ids);
-    if constexpr (NET_AHEAD) {  // the first group's network now, the others' one group ahead
-        store_net();
-        __syncthreads();
-        run_net(g);
-        if (gn < ngroups) load_net(gn);
-    }
 
     int s = 0;
     for (; g < ngroups; g = gn, gn += stride, s = NBUF == 2 ? s ^ 1 : 0) {
@@ -689,17 +560,12 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
         real Hm[MP][9], gv[MP];
         if (!LATE) load_metric(g, Hm, gv);
         if (NBUF == 2 && gn < ngroups) store_ids(ids, sNode + (s ^ 1) * NPL);
-        if (!NET_AHEAD) store_net();
         cp_async_wait_all();
         __syncthreads();
-        if (gn < ngroups) {
-            if (NBUF == 2) {
-                gather(gn, sNode + (s ^ 1) * NPL, sF + (s ^ 1) * NDF * NPL);
-                if (gn + stride < ngroups) load_ids(gn + stride, ids);
-            }
-            if (!NET_AHEAD) load_net(gn);
+        if (NBUF == 2 && gn < ngroups) {
+            gather(gn, sNode + (s ^ 1) * NPL, sF + (s ^ 1) * NDF * NPL);
+            if (gn + stride < ngroups) load_ids(gn + stride, ids);
         }
-        if (!NET_AHEAD) run_net(g);
         if constexpr (FUSEZ) {
             if (lt0.active) grad_pass<G, 0>(lt0, sFs, sX, sD);
             if (lt1.active) grad_pass<G, 1>(lt1, sFs, sX, sD);
@@ -863,14 +729,6 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
             __syncthreads();
             gather(gn, sNode, sF);
             if (gn + stride < ngroups) load_ids(gn + stride, ids);
-            if constexpr (NET_AHEAD) {
-                // The next group's network while its node fields are in flight
-                // (this group's viscosities were last read in its zeta stage).
-                store_net();
-                __syncthreads();
-                run_net(gn);
-                if (gn + stride < ngroups) load_net(gn + stride);
-            }
         }
     }
 }
@@ -879,7 +737,7 @@ template <typename real, int P, int VISC>
 cudaError_t launch_diffu_pn(const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
     using G = DiffuGeom<real, P>;
-    constexpr size_t smem = diffu_smem_bytes<G>() + (VISC == VISC_NET ? net_smem_floats<G>() * sizeof(float) : 0);
+    constexpr size_t smem = diffu_smem_bytes<G>();
     static_assert(smem <= 227 * 1024, "shared memory budget");
     static_assert(G::NE >= 1, "element group");
     auto kern = diffu_kernel<G, VISC>;
@@ -896,17 +754,13 @@ cudaError_t launch_diffu_pn(const DiffuArgs<real> &a, const TableScratch *tabs, 
     const int grid = persistent_grid(kern, G::NT, smem, ngroups);
     if (grid <= 0) return cudaErrorInvalidConfiguration;
     kern<<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, ngroups, a.connec, a.He, a.gpvol, tabs, a.Cp, a.Pr, a.rho, a.u,
-                                    a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.nu_elem, a.Rmass, a.Rmom, a.Rener, a.net);
+                                    a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.nu_elem, a.Rmass, a.Rmom, a.Rener);
     return cudaGetLastError();
 }
 
 template <typename real, int P>
 cudaError_t launch_diffu_p(const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st)
 {
-    if (a.net.feat) {
-        if (sizeof(real) != 4) return cudaErrorInvalidValue;  // the network path is FP32
-        return launch_diffu_pn<real, P, VISC_NET>(a, tabs, st);
-    }
     if (a.nu_elem) return launch_diffu_pn<real, P, VISC_NU_ELEM>(a, tabs, st);
     return launch_diffu_pn<real, P, VISC_MU_E>(a, tabs, st);
 }

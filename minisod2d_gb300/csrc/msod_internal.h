@@ -31,13 +31,4 @@ int mode_diffusion(int porder, int nelem, int npoin, const int *connec, const fl
                    const float *mu_fluid, const float *mu_e, const float *mu_sgs, float *Rmass, float *Rmom,
                    float *Rener, void *stream);
 
-struct DiffuNet;
-// The FP32 diffusion call with the viscosity taken from the per-element
-// network in the kernel's prologue (argument checks, output zeroing, tables).
-int diffusion_with_net(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
-                       const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
-                       const int *gmshAtoK, float Cp, float Pr, const float *rho, const float *u, const float *Tem,
-                       const float *mu_fluid, const float *mu_sgs, const DiffuNet &net, float *Rmass, float *Rmom,
-                       float *Rener, void *stream);
-
 }  // namespace msod

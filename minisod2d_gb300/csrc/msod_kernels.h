@@ -88,24 +88,11 @@ struct ConvecArgs : ElementArgs<real> {
 
 struct MlpNorm;
 
-// The per-element network evaluated in the diffusion prologue (FP32 kernels):
-// nu(e) = numax(e) 10^-s(feat(e)) where flag(e) == 0, nu_fb(e) (the plain
-// estimator's value) where flag(e) != 0; nu_out, if set, receives nu.
-struct DiffuNet {
-    const float *feat;
-    const __half *wh;
-    const MlpNorm *norm;
-    const float *numax, *nu_fb;
-    const int *flag;
-    float *nu_out;
-};
-
 template <typename real>
 struct DiffuArgs : ElementArgs<real> {
     real Cp, Pr;
     const real *rho, *u, *Tem, *mu_fluid, *mu_e, *mu_sgs;
     const real *nu_elem;  // if set: mu_e(e, a) = rho(a) * nu_elem[e] and mu_e is not read
-    DiffuNet net{};       // if net.feat is set: nu from the network, mu_e and nu_elem are not read
     real *Rmass, *Rmom, *Rener;
 };
 
@@ -207,7 +194,9 @@ struct ViscArgs {
     float Rgas, gamma, ce, cmax;
     int normalise;
     const EntropyStats *stats;
-    const int *only;     // if set: process only elements with only[e] != 0, write nu only
+    // If set: process only the elements list[0 .. *count) (the compacted list
+    // of flagged elements written by launch_mlp_predict), write nu only.
+    const int *list, *count;
     float *mu_e, *nu, *numax;
     const TableScratch *tabs;  // the call's element tables (table_prep_kernel)
 };
@@ -221,16 +210,16 @@ struct FeatureArgs {
     float Rgas, gamma, cmax;
     const EntropyStats *stats;
     float *feat, *numax;
-    const MlpNorm *norm;  // with flag: flag[e] = 1 where a feature leaves the training range
-    int *flag;
 };
 
 cudaError_t launch_entropy_stats(int npoin, const float *rho, const float *p_or_T, float Rgas, float gamma,
                                  EntropyStats *st, cudaStream_t s);
 cudaError_t launch_entropy_visc(int porder, const ViscArgs &a, cudaStream_t st);
 cudaError_t launch_features(int porder, const FeatureArgs &a, cudaStream_t st);
+// y = 10^-s, nu = y numax (if nu), flag = 1 outside the training range (if
+// flag); with list: list[0 .. *count) = the flagged elements (any order).
 cudaError_t launch_mlp_predict(int nelem, const float *feat, const __half *wh, const MlpNorm *nm, const float *numax,
-                               float *y, float *nu, int *flag, cudaStream_t st);
+                               float *y, float *nu, int *flag, int *list, int *count, cudaStream_t st);
 cudaError_t launch_mlp_norm(int n, const float *feat, MlpNorm *nm, cudaStream_t st);
 cudaError_t launch_mlp_grad(int n, const float *feat, const float *target, const float *weight, const int *idx,
                             int batch, uint32_t seed,

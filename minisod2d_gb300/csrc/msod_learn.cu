@@ -59,7 +59,7 @@ void *scratch(int slot, size_t bytes)
     }
     return s.p;
 }
-enum { SLOT_STATS = 0, SLOT_TABLES, SLOT_FEAT, SLOT_NUMAX, SLOT_NU, SLOT_Y, SLOT_FLAG };
+enum { SLOT_STATS = 0, SLOT_TABLES, SLOT_FEAT, SLOT_NUMAX, SLOT_NU, SLOT_LIST, SLOT_COUNT };
 
 int geometry_ok(int porder, int nelem, int npoin, const void *connec, const void *He, const void *gpvol,
                 const void *dlx, const void *inv, const void *ai, const void *aj, const void *ak)
@@ -159,7 +159,7 @@ int msod_entropy_viscosity(int porder, int nelem, int npoin, const int *connec, 
     a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlxigp_ip;
     a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
     a.rho = rho; a.u = u; a.p_or_T = pr; a.Rgas = 0.0f; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
-    a.normalise = normalise; a.stats = stats; a.only = nullptr; a.mu_e = mu_e; a.nu = nu_elem; a.numax = numax_elem;
+    a.normalise = normalise; a.stats = stats; a.list = nullptr; a.count = nullptr; a.mu_e = mu_e; a.nu = nu_elem; a.numax = numax_elem;
     a.tabs = tabs;
     return cuda_rc(launch_entropy_visc(porder, a, st), "entropy viscosity launch");
 }
@@ -168,8 +168,7 @@ int msod_entropy_viscosity(int porder, int nelem, int npoin, const int *connec, 
 static int features_impl(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
                          const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
                          const int *gmshAtoK, const float *rho, const float *u, const float *p_or_T, float Rgas,
-                         float gamma, float cmax, float *feat, float *numax_elem, const MlpNorm *norm, int *flag,
-                         void *stream);
+                         float gamma, float cmax, float *feat, float *numax_elem, void *stream);
 
 int msod_mlp_features(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
                       const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
@@ -178,14 +177,13 @@ int msod_mlp_features(int porder, int nelem, int npoin, const int *connec, const
 {
     clear_error();
     return features_impl(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
-                         rho, u, p_or_T, Rgas, gamma, cmax, feat, numax_elem, nullptr, nullptr, stream);
+                         rho, u, p_or_T, Rgas, gamma, cmax, feat, numax_elem, stream);
 }
 
 static int features_impl(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
                          const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
                          const int *gmshAtoK, const float *rho, const float *u, const float *p_or_T, float Rgas,
-                         float gamma, float cmax, float *feat, float *numax_elem, const MlpNorm *norm, int *flag,
-                         void *stream)
+                         float gamma, float cmax, float *feat, float *numax_elem, void *stream)
 {
     int rc = geometry_ok(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK);
     if (rc) return rc;
@@ -201,7 +199,7 @@ static int features_impl(int porder, int nelem, int npoin, const int *connec, co
     FeatureArgs fa{};
     fa.nelem = nelem; fa.npoin = npoin; fa.connec = connec; fa.He = He; fa.gpvol = gpvol; fa.tabs = tabs;
     fa.rho = rho; fa.u = u; fa.p_or_T = p_or_T; fa.Rgas = Rgas; fa.gamma = gamma; fa.cmax = cmax; fa.stats = stats;
-    fa.feat = feat; fa.numax = numax_elem; fa.norm = norm; fa.flag = flag;
+    fa.feat = feat; fa.numax = numax_elem;
     return cuda_rc(launch_features(porder, fa, st), "feature launch");
 }
 
@@ -341,7 +339,7 @@ int msod_mlp_predict(const msod_mlp *m, const float *feat, const float *numax_el
     clear_error();
     if (!m || !feat || nelem < 1 || !y) return set_error(MSOD_ERR_INVALID_ARG, "bad prediction arguments");
     if (nu_elem && !numax_elem) return set_error(MSOD_ERR_INVALID_ARG, "nu needs numax");
-    return cuda_rc(launch_mlp_predict(nelem, feat, m->wh, m->norm, numax_elem, y, nu_elem, flag,
+    return cuda_rc(launch_mlp_predict(nelem, feat, m->wh, m->norm, numax_elem, y, nu_elem, flag, nullptr, nullptr,
                                       static_cast<cudaStream_t>(stream)),
                    "prediction launch");
 }
@@ -412,6 +410,39 @@ int msod_mlp_load(msod_mlp *m, const char *path)
     return rc;
 }
 
+// The learned viscosity into nu (nelem): the features kernel, then the
+// prediction kernel (nu = 10^-s nu_max, the trusted-range flags, and the
+// flagged elements as a compacted list), then the plain estimator over that
+// list only, overwriting nu there -- its work follows the number of flagged
+// elements (a shock band spread over many element groups would otherwise cost
+// most of a full estimator pass).
+static int learned_nu(const msod_mlp *m, int porder, int nelem, int npoin, const int *connec, const float *He,
+                      const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI,
+                      const int *gmshAtoJ, const int *gmshAtoK, const float *rho, const float *u, const float *p_or_T,
+                      float Rgas, float gamma, float ce, float cmax, float *nu, int *flag, void *stream)
+{
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float *feat = static_cast<float *>(scratch(SLOT_FEAT, sizeof(float) * kMlpIn * (size_t)nelem));
+    float *numax = static_cast<float *>(scratch(SLOT_NUMAX, sizeof(float) * (size_t)nelem));
+    int *list = static_cast<int *>(scratch(SLOT_LIST, sizeof(int) * (size_t)nelem));
+    int *count = static_cast<int *>(scratch(SLOT_COUNT, sizeof(int)));
+    if (!feat || !numax || !list || !count) return set_error(MSOD_ERR_CUDA, "could not allocate per-element scratch");
+    int rc = features_impl(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
+                           gmshAtoK, rho, u, p_or_T, Rgas, gamma, cmax, feat, numax, stream);
+    if (rc) return rc;
+    rc = cuda_rc(launch_mlp_predict(nelem, feat, m->wh, m->norm, numax, nullptr, nu, flag, list, count, st),
+                 "prediction launch");
+    if (rc) return rc;
+    EntropyStats *stats = static_cast<EntropyStats *>(scratch(SLOT_STATS, sizeof(EntropyStats)));
+    ViscArgs a{};
+    a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlxigp_ip;
+    a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
+    a.rho = rho; a.u = u; a.p_or_T = p_or_T; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
+    a.normalise = 1; a.stats = stats; a.list = list; a.count = count; a.mu_e = nullptr; a.nu = nu; a.numax = nullptr;
+    a.tabs = prepared_tables(porder);  // prepared by the feature call above
+    return cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
+}
+
 int msod_learned_viscosity(const msod_mlp *m, int porder, int nelem, int npoin, const int *connec, const float *He,
                            const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK, const int *gmshAtoI,
                            const int *gmshAtoJ, const int *gmshAtoK, const float *rho, const float *u,
@@ -423,26 +454,8 @@ int msod_learned_viscosity(const msod_mlp *m, int porder, int nelem, int npoin, 
     int rc = geometry_ok(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK);
     if (rc) return rc;
     if (!rho || !u || !p_or_T || !nu_elem) return set_error(MSOD_ERR_INVALID_ARG, "NULL field or nu");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    float *feat = static_cast<float *>(scratch(SLOT_FEAT, sizeof(float) * kMlpIn * (size_t)nelem));
-    float *numax = static_cast<float *>(scratch(SLOT_NUMAX, sizeof(float) * (size_t)nelem));
-    float *y = static_cast<float *>(scratch(SLOT_Y, sizeof(float) * (size_t)nelem));
-    int *fl = flag ? flag : static_cast<int *>(scratch(SLOT_FLAG, sizeof(int) * (size_t)nelem));
-    if (!feat || !numax || !y || !fl) return set_error(MSOD_ERR_CUDA, "could not allocate per-element scratch");
-    rc = msod_mlp_features(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
-                           gmshAtoK, rho, u, p_or_T, Rgas, gamma, cmax, feat, numax, stream);
-    if (rc) return rc;
-    rc = cuda_rc(launch_mlp_predict(nelem, feat, m->wh, m->norm, numax, y, nu_elem, fl, st), "prediction launch");
-    if (rc) return rc;
-    // Per-element fallback: the plain estimator where a feature left the training range.
-    EntropyStats *stats = static_cast<EntropyStats *>(scratch(SLOT_STATS, sizeof(EntropyStats)));
-    ViscArgs a{};
-    a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlxigp_ip;
-    a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
-    a.rho = rho; a.u = u; a.p_or_T = p_or_T; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
-    a.normalise = 1; a.stats = stats; a.only = fl; a.mu_e = nullptr; a.nu = nu_elem; a.numax = nullptr;
-    a.tabs = prepared_tables(porder);  // prepared by the feature call above
-    return cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
+    return learned_nu(m, porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                      rho, u, p_or_T, Rgas, gamma, ce, cmax, nu_elem, flag, stream);
 }
 
 int msod_diffusion_ijk_learned(const msod_mlp *m, int porder, int nelem, int npoin, const int *connec,
@@ -459,32 +472,13 @@ int msod_diffusion_ijk_learned(const msod_mlp *m, int porder, int nelem, int npo
     int rc = geometry_ok(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK);
     if (rc) return rc;
     if (!rho || !u || !Tem || !p_or_T) return set_error(MSOD_ERR_INVALID_ARG, "NULL field");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    float *feat = static_cast<float *>(scratch(SLOT_FEAT, sizeof(float) * kMlpIn * (size_t)nelem));
-    float *numax = static_cast<float *>(scratch(SLOT_NUMAX, sizeof(float) * (size_t)nelem));
-    float *nu_fb = static_cast<float *>(scratch(SLOT_NU, sizeof(float) * (size_t)nelem));
-    int *fl = flag ? flag : static_cast<int *>(scratch(SLOT_FLAG, sizeof(int) * (size_t)nelem));
-    if (!feat || !numax || !nu_fb || !fl) return set_error(MSOD_ERR_CUDA, "could not allocate per-element scratch");
-    // 1. features and the out-of-range flags
-    rc = features_impl(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
-                       rho, u, p_or_T, Rgas, gamma, cmax, feat, numax, m->norm, fl, stream);
+    float *nu = nu_elem ? nu_elem : static_cast<float *>(scratch(SLOT_NU, sizeof(float) * (size_t)nelem));
+    if (!nu) return set_error(MSOD_ERR_CUDA, "could not allocate the per-element viscosity");
+    rc = learned_nu(m, porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, rho,
+                    u, p_or_T, Rgas, gamma, ce, cmax, nu, flag, stream);
     if (rc) return rc;
-    // 2. the plain estimator on the flagged elements only (per-element fallback)
-    EntropyStats *stats = static_cast<EntropyStats *>(scratch(SLOT_STATS, sizeof(EntropyStats)));
-    ViscArgs a{};
-    a.nelem = nelem; a.npoin = npoin; a.connec = connec; a.He = He; a.gpvol = gpvol; a.dlxigp_ip = dlxigp_ip;
-    a.invAtoIJK = invAtoIJK; a.AtoI = gmshAtoI; a.AtoJ = gmshAtoJ; a.AtoK = gmshAtoK;
-    a.rho = rho; a.u = u; a.p_or_T = p_or_T; a.Rgas = Rgas; a.gamma = gamma; a.ce = ce; a.cmax = cmax;
-    a.normalise = 1; a.stats = stats; a.only = fl; a.mu_e = nullptr; a.nu = nu_fb; a.numax = nullptr;
-    a.tabs = prepared_tables(porder);  // prepared by the feature call above
-    rc = cuda_rc(launch_entropy_visc(porder, a, st), "fallback estimator launch");
-    if (rc) return rc;
-    // 3. the diffusion, with the network evaluated in its prologue
-    DiffuNet net{};
-    net.feat = feat; net.wh = m->wh; net.norm = m->norm; net.numax = numax; net.nu_fb = nu_fb; net.flag = fl;
-    net.nu_out = nu_elem;
-    return diffusion_with_net(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
-                              gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_sgs, net, Rmass, Rmom, Rener, stream);
+    return msod_diffusion_ijk_nu(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
+                                 gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, nu, mu_sgs, Rmass, Rmom, Rener, stream);
 }
 
 }  // extern "C"

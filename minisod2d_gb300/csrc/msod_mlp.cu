@@ -59,19 +59,27 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
                     const float *__restrict__ gpvol, const TableScratch *__restrict__ tabs,
                     const float *__restrict__ rho, const float *__restrict__ u, const float *__restrict__ p_or_T,
                     float Rgas, float gamma, float cmax, const EntropyStats *__restrict__ st,
-                    float *__restrict__ feat, float *__restrict__ numax_out, const MlpNorm *__restrict__ norm,
-                    int *__restrict__ flag)
+                    float *__restrict__ feat, float *__restrict__ numax_out)
 {
     constexpr int Q = P + 1, N = Q * Q * Q, kFeatWarps = feat_warps<P>();
     constexpr int NPL = (N + 31) / 32;  // nodes per lane
-    __shared__ float sv[kFeatWarps][5][N];  // rho, p, u0, u1, u2 by gmsh node
-    __shared__ int sPerm[N];                // lattice -> gmsh node
-    __shared__ float sD[3 * Q * Q];         // 1-D derivative matrices
+    // rho, p, u0, u1, u2 by lattice point l = (K*Q+J)*Q+I (SOD 1-D indices);
+    // plane 0 first holds the element's node ids by gmsh node.
+    __shared__ float sv[kFeatWarps][5][N];
+    __shared__ int sPerm[N];         // lattice -> gmsh node
+    __shared__ float sD[3 * Q * Q];  // 1-D derivative matrices
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int e = blockIdx.x * kFeatWarps + w;
+    const int e0 = blockIdx.x * kFeatWarps, e = e0 + w;
     const TableScratch *t = tabs;
     for (int i = threadIdx.x; i < N; i += 32 * kFeatWarps) sPerm[i] = t->perm[i];
     for (int i = threadIdx.x; i < 3 * Q * Q; i += 32 * kFeatWarps) sD[i] = t->Df[i];
+    // The block's node ids, element-fastest as connec stores them (the block's
+    // elements share each 32-byte sector).
+    for (int i = threadIdx.x; i < kFeatWarps * N; i += 32 * kFeatWarps) {
+        const int el = i % kFeatWarps, a = i / kFeatWarps;
+        const int id = e0 + el < nelem ? ldg(connec + (size_t)a * nelem + e0 + el) - 1 : 0;
+        reinterpret_cast<int *>(sv[el][0])[a] = min(max(id, 0), npoin - 1);
+    }
     __syncthreads();
     if (e >= nelem) return;
     // Entropy normalisation (read early: its latency hides behind the gathers).
@@ -84,29 +92,31 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
     const float s_scale = 0.69314718f / (gamma - 1.0f);  // ln 2 / (gamma - 1): s from base-2 logarithms
     // All of the lane's node ids first, then every field load of the lane, then
     // the arithmetic: the loads overlap (15-17 % faster than loads interleaved
-    // with the per-node statistics).
+    // with the per-node statistics).  Lanes take the lattice points in order,
+    // so a warp's loads follow the mesh lines (x-neighbours share sectors).
     int pn[NPL];
 #pragma unroll
     for (int k = 0; k < NPL; ++k) {
-        const int a = lane + 32 * k;
-        pn[k] = a < N ? min(max(ldg(connec + (size_t)a * nelem + e) - 1, 0), npoin - 1) : 0;
+        const int l = lane + 32 * k;
+        pn[k] = l < N ? reinterpret_cast<const int *>(sv[w][0])[sPerm[l]] : 0;
     }
+    __syncwarp();  // every id read before plane 0 takes the density
     float fr[NPL], fp[NPL], fx[NPL], fy[NPL], fz[NPL];
 #pragma unroll
     for (int k = 0; k < NPL; ++k) {
-        const int a = lane + 32 * k;
+        const int l = lane + 32 * k;
         const int p = pn[k];
-        const bool ok = a < N;
+        const bool ok = l < N;
         fr[k] = ok ? ldg(rho + p) : 1.0f;
         fp[k] = ok ? ldg(p_or_T + p) : 1.0f;
         fx[k] = ok ? ldg(u + p) : 0.0f;
         fy[k] = ok ? ldg(u + np + p) : 0.0f;
         fz[k] = ok ? ldg(u + 2 * np + p) : 0.0f;
-        vol += ok ? ldg(gpvol + (size_t)e * N + a) : 0.0f;
+        vol += ok ? ldg(gpvol + (size_t)e * N + l) : 0.0f;  // the sum over all of the element's points
     }
 #pragma unroll
     for (int k = 0; k < NPL; ++k) {
-        const int a = lane + 32 * k;
+        const int a = lane + 32 * k;  // lattice point
         if (a >= N) break;
         const float r = fr[k];
         const float pr = Rgas > 0.0f ? r * Rgas * fp[k] : fp[k];
@@ -144,7 +154,7 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
     // Centre node and the natural -> SOD 1-D index map (0 -> 0, P -> 1, k -> k+1).
     const int mnat = P / 2;
     const int ms = mnat == 0 ? 0 : (mnat == P ? 1 : mnat + 1);
-    auto node = [&](int I, int J, int K) { return sPerm[(K * Q + J) * Q + I]; };
+    auto node = [&](int I, int J, int K) { return (K * Q + J) * Q + I; };  // lattice point (planes of sv)
     const int nat[3] = {0, ms, 1};  // SOD positions of natural 0, mid, P
     // Lanes 0-8: iso derivative gi[i][d] of u_i along d at the centre (lane 3i + d);
     // lanes 9-11: second differences and product-rule defect along d = lane - 9;
@@ -175,7 +185,7 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
         const float B = ev[1] * (uv[2] - uv[0]) + uv[1] * (ev[2] - ev[0]);
         def_l = fabsf(A - B);
     } else if (lane < 21) {
-        hval = ldg(He + ((size_t)e * N + node(ms, ms, ms)) * 9 + (lane - 12));
+        hval = ldg(He + ((size_t)e * N + sPerm[node(ms, ms, ms)]) * 9 + (lane - 12));
     }
     float gi[3][3], Hc[9];
 #pragma unroll
@@ -223,12 +233,6 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
     f[10] = flog((emax - emin) / neta);
     f[11] = flog(defect / (neta * (umean + cmean)));
     if (numax_out) numax_out[e] = cmax * h * spdmax;
-    if (flag) {  // outside the network's training range: the plain estimator takes over
-        int out = 0;
-        for (int k = 0; k < kMlpIn; ++k)
-            if (!(f[k] >= norm->fmin[k] && f[k] <= norm->fmax[k])) out = 1;
-        flag[e] = out;
-    }
 }
 
 template <int P>
@@ -238,7 +242,7 @@ cudaError_t features_p(const FeatureArgs &a, cudaStream_t st)
     const unsigned grid = (unsigned)((a.nelem + kFeatWarps - 1) / kFeatWarps);
     features_kernel<P><<<grid, 32 * kFeatWarps, 0, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.tabs, a.rho,
                                                          a.u, a.p_or_T, a.Rgas, a.gamma, a.cmax, a.stats, a.feat,
-                                                         a.numax, a.norm, a.flag);
+                                                         a.numax);
     return cudaGetLastError();
 }
 
@@ -277,7 +281,8 @@ __device__ __forceinline__ void mlp_forward(const float *__restrict__ w, const M
 // Inference: y = 10^-s in (0, 1] and the out-of-range flag per element.
 __global__ void mlp_predict_kernel(int nelem, const float *__restrict__ feat, const __half *__restrict__ wh,
                                    const MlpNorm *__restrict__ nm, const float *__restrict__ numax,
-                                   float *__restrict__ y, float *__restrict__ nu, int *__restrict__ flag)
+                                   float *__restrict__ y, float *__restrict__ nu, int *__restrict__ flag,
+                                   int *__restrict__ list, int *count)
 {
     __shared__ float w[kMlpParams];
     __shared__ MlpNorm snm;
@@ -285,20 +290,20 @@ __global__ void mlp_predict_kernel(int nelem, const float *__restrict__ feat, co
     if (threadIdx.x == 0) snm = *nm;
     __syncthreads();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nelem) return;
-    float x[kMlpIn];
     int out = 0;
+    if (e < nelem) {
+        float x[kMlpIn];
 #pragma unroll
-    for (int k = 0; k < kMlpIn; ++k) {
-        x[k] = feat[(size_t)e * kMlpIn + k];
-        if (!(x[k] >= snm.fmin[k] && x[k] <= snm.fmax[k])) out = 1;
+        for (int k = 0; k < kMlpIn; ++k) {
+            x[k] = feat[(size_t)e * kMlpIn + k];
+            if (!(x[k] >= snm.fmin[k] && x[k] <= snm.fmax[k])) out = 1;
+        }
+        const float yy = y_from_s(mlp_infer(w, snm, x));
+        if (y) y[e] = yy;
+        if (nu) nu[e] = yy * numax[e];
+        if (flag) flag[e] = out;
     }
-    Act s;
-    mlp_forward(w, snm, x, s);
-    const float yy = y_from_s(s.y);
-    y[e] = yy;
-    if (nu) nu[e] = yy * numax[e];
-    if (flag) flag[e] = out;
+    if (list) warp_append(out != 0, e, list, count);  // every lane of the warp (the block is whole warps)
 }
 
 // Per-feature mean, 1/std, min, max over the training samples (one block per feature).
@@ -457,9 +462,13 @@ cudaError_t launch_features(int porder, const FeatureArgs &a, cudaStream_t st)
 }
 
 cudaError_t launch_mlp_predict(int nelem, const float *feat, const __half *wh, const MlpNorm *nm, const float *numax,
-                               float *y, float *nu, int *flag, cudaStream_t st)
+                               float *y, float *nu, int *flag, int *list, int *count, cudaStream_t st)
 {
-    mlp_predict_kernel<<<(nelem + 127) / 128, 128, 0, st>>>(nelem, feat, wh, nm, numax, y, nu, flag);
+    if (list) {
+        const cudaError_t err = cudaMemsetAsync(count, 0, sizeof(int), st);
+        if (err != cudaSuccess) return err;
+    }
+    mlp_predict_kernel<<<(nelem + 127) / 128, 128, 0, st>>>(nelem, feat, wh, nm, numax, y, nu, flag, list, count);
     return cudaGetLastError();
 }
 

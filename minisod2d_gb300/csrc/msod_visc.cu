@@ -45,14 +45,28 @@ __global__ void entropy_stats_kernel(int npoin, const float *__restrict__ rho, c
                                      float Rgas, float gamma, EntropyStats *st)
 {
     float s = 0.0f, mn = 3.0e38f, mx = -3.0e38f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npoin; i += gridDim.x * blockDim.x) {
-        const float r = ldg(rho + i);
-        const float p = Rgas > 0.0f ? r * Rgas * ldg(p_or_T + i) : ldg(p_or_T + i);
+    auto add = [&](float r, float q) {
+        const float p = Rgas > 0.0f ? r * Rgas * q : q;
         const float eta = r / (gamma - 1.0f) * (logf(p) - gamma * logf(r));
         s += eta;
         mn = fminf(mn, eta);
         mx = fmaxf(mx, eta);
+    };
+    // Four grid strides per trip, every load issued before the arithmetic
+    // (eight loads in flight per thread instead of two).
+    const int G = gridDim.x * blockDim.x;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i < npoin - 3 * G; i += 4 * G) {
+        float r[4], q[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            r[k] = ldg(rho + i + k * G);
+            q[k] = ldg(p_or_T + i + k * G);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) add(r[k], q[k]);
     }
+    for (; i < npoin; i += G) add(ldg(rho + i), ldg(p_or_T + i));
     // Warp, then block reduction: one set of global atomics per block (the
     // atomics on these three words serialise in L2).
     double sd = (double)s;
@@ -164,9 +178,9 @@ __global__ void __launch_bounds__(G::NT)
     entropy_visc_kernel(int nelem, int npoin, const int *__restrict__ connec, const float *__restrict__ He,
                         const float *__restrict__ gpvol, const float *__restrict__ rho, const float *__restrict__ u,
                         const float *__restrict__ p_or_T, float Rgas, float gamma, float ce, float cmax,
-                        int normalise, const EntropyStats *__restrict__ st, const int *__restrict__ only,
-                        float *__restrict__ mu_e, float *__restrict__ nu_out, float *__restrict__ numax_out,
-                        const TableScratch *__restrict__ tabs)
+                        int normalise, const EntropyStats *__restrict__ st, const int *__restrict__ list,
+                        const int *__restrict__ count, float *__restrict__ mu_e, float *__restrict__ nu_out,
+                        float *__restrict__ numax_out, const TableScratch *__restrict__ tabs)
 {
     constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT, NPL = G::NPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -176,22 +190,19 @@ __global__ void __launch_bounds__(G::NT)
     int *sNode = reinterpret_cast<int *>(sD + 3 * Q * Q);
     int *sPerm = sNode + NPL;
     int *sLat = sPerm + N;
-    __shared__ int s_kS[NE];
+    __shared__ int s_kS[NE], s_eid[NE];
     __shared__ float s_vol[NE], s_nu[NE];
 
     const int tid = threadIdx.x;
-    const int e0 = blockIdx.x * NE;
-    if (only) {  // fallback mode: only groups with a flagged element do any work
-        __shared__ int s_any;
-        if (tid == 0) {
-            int any = 0;
-            for (int el = 0; el < NE; ++el)
-                if (e0 + el < nelem && only[e0 + el]) any = 1;
-            s_any = any;
-        }
-        __syncthreads();
-        if (!s_any) return;
-    }
+    // The block's elements: e0 .. e0+NE-1 (one group per block), or in list
+    // mode (the per-element fallback) the entries e0 .. of the compacted list,
+    // the blocks striding over the list's groups; -1 beyond the end.
+    const int nwork = list ? ldg(count) : nelem;
+    for (int gb = blockIdx.x; gb * NE < nwork; gb += gridDim.x) {
+    const int e0 = gb * NE;
+    __syncthreads();  // the previous group's shared-memory reads are complete
+    if (tid < NE) s_eid[tid] = e0 + tid < nwork ? (list ? ldg(list + e0 + tid) : e0 + tid) : -1;
+    __syncthreads();
     // Node ids of the group (connec is element-fastest) into registers while
     // the call's tables are copied into shared memory.
     constexpr int IPT = (NE * N + NT - 1) / NT;
@@ -199,8 +210,8 @@ __global__ void __launch_bounds__(G::NT)
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
         const int i = tid + k * NT;
-        const int el = i % NE, a = i / NE, e = e0 + el;
-        ids[k] = (i < NE * N && e < nelem) ? ldg(connec + (size_t)a * nelem + e) - 1 : -1;
+        const int el = i % NE, a = i / NE, e = s_eid[el];
+        ids[k] = (i < NE * N && e >= 0) ? ldg(connec + (size_t)a * nelem + e) - 1 : -1;
     }
     for (int i = tid; i < N; i += NT) {
         sPerm[i] = tabs->perm[i];
@@ -249,10 +260,10 @@ __global__ void __launch_bounds__(G::NT)
     {
         const int lane = tid & 31, warp = tid >> 5;
         for (int el = warp; el < NE; el += NT / 32) {
-            const int ee = e0 + el;
+            const int ee = s_eid[el];
             unsigned mx = 0u;
             float vol = 0.0f;
-            if (ee < nelem)
+            if (ee >= 0)
                 for (int l = lane; l < N; l += 32) {
                     const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
                     mx = max(mx, __float_as_uint(sR[o]));  // non-negative floats order like their bits
@@ -269,8 +280,8 @@ __global__ void __launch_bounds__(G::NT)
     }
     __syncthreads();
     const LineThread<G> lt(tid);
-    const int e = e0 + lt.el;
-    const bool live = lt.active && e < nelem;
+    const int e = s_eid[lt.el];
+    const bool live = lt.active && e >= 0;
     if (live) residual_pass<G, 0>(lt, sF, sR, sPerm, sD, He, e, gamma);
     __syncthreads();
     if (live) residual_pass<G, 1>(lt, sF, sR, sPerm, sD, He, e, gamma);
@@ -288,9 +299,9 @@ __global__ void __launch_bounds__(G::NT)
     {
         const int lane = tid & 31, warp = tid >> 5;
         for (int el = warp; el < NE; el += NT / 32) {
-            const int ee = e0 + el;
+            const int ee = s_eid[el];
             unsigned mx = 0u;
-            if (ee < nelem)
+            if (ee >= 0)
                 for (int l = lane; l < N; l += 32) {
                     const int o = el * ES + (l / (Q * Q) * Q + (l / Q) % Q) * QP + l % Q;
                     mx = max(mx, __float_as_uint(fabsf(sR[o])));
@@ -302,23 +313,23 @@ __global__ void __launch_bounds__(G::NT)
                 const float nuE = ce * h * h * __uint_as_float(mx) / neta;
                 const float nu = fminf(numax, nuE);
                 s_nu[el] = nu;
-                if (ee < nelem) {
-                    if (only) {
-                        if (only[ee]) nu_out[ee] = nu;
-                    } else {
-                        if (nu_out) nu_out[ee] = nu;
-                        if (numax_out) numax_out[ee] = numax;
-                    }
+                if (ee >= 0) {
+                    if (nu_out) nu_out[ee] = nu;
+                    if (numax_out && !list) numax_out[ee] = numax;
                 }
             }
         }
     }
-    if (only || !mu_e) return;
-    __syncthreads();
-    for (int i = tid; i < NE * N; i += NT) {
-        const int el = i % NE, a = i / NE, ee = e0 + el;
-        if (ee >= nelem) continue;
-        mu_e[(size_t)a * nelem + ee] = sF[V_RHO * NPL + el * ES + sLat[a]] * s_nu[el];
+    if (list) continue;
+    if (mu_e) {
+        __syncthreads();
+        for (int i = tid; i < NE * N; i += NT) {
+            const int el = i % NE, a = i / NE, ee = s_eid[el];
+            if (ee < 0) continue;
+            mu_e[(size_t)a * nelem + ee] = sF[V_RHO * NPL + el * ES + sLat[a]] * s_nu[el];
+        }
+    }
+    break;  // one group per block outside list mode
     }
 }
 
@@ -354,10 +365,14 @@ cudaError_t visc_p(const ViscArgs &a, cudaStream_t st)
                                       cudaMemcpyDeviceToDevice, st);
         if (err != cudaSuccess) return err;
     }
-    const unsigned grid = (unsigned)((a.nelem + G::NE - 1) / G::NE);
+    // List mode: resident blocks stride over the list (its length is known on
+    // the device only); otherwise one group per block.
+    const int ngroups = (a.nelem + G::NE - 1) / G::NE;
+    const unsigned grid = (unsigned)(a.list ? persistent_grid(kern, G::NT, smem, ngroups) : ngroups);
+    if (grid == 0) return cudaErrorInvalidConfiguration;
     kern<<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, a.connec, a.He, a.gpvol, a.rho, a.u, a.p_or_T, a.Rgas, a.gamma,
                                     a.ce, a.cmax, a.normalise,
-                                    a.stats, a.only, a.mu_e, a.nu, a.numax, a.tabs);
+                                    a.stats, a.list, a.count, a.mu_e, a.nu, a.numax, a.tabs);
     return cudaGetLastError();
 }
 

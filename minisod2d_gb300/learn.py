@@ -150,9 +150,10 @@ def learned_viscosity(mlp, dev, nu=None, flag=None, ce=CE, cmax=CMAX, gamma=GAMM
 
 def diffusion_learned(mlp, dev, out=None, nu=None, flag=None, ce=CE, cmax=CMAX, gamma=GAMMA, from_T=False,
                       stream=None):
-    """Diffusion with the network evaluated in the diffusion kernel's prologue
-    (features from rho, u and the pressure, or p = rho Rgas T with ``from_T``;
-    plain-estimator fallback per element).  Returns the residuals, the
+    """Diffusion with the learned viscosity in one call (msod_diffusion_ijk_learned:
+    the learned viscosity -- features from rho, u and the pressure, or
+    p = rho Rgas T with ``from_T``; plain-estimator fallback per element --
+    then the per-element-viscosity diffusion).  Returns the residuals, the
     viscosity used and the fallback flags."""
     import torch
 
@@ -301,8 +302,8 @@ def evaluate(mlp, dev, ybar=None, reps=5):
     r["ms_learned_estimator"] = _event_ms(lambda: learned_viscosity(mlp, dev, nu_lb, flag_b), reps)
     r["ms_plain_estimator_plus_diffusion"] = _event_ms(plain, reps)
     r["ms_learned_estimator_plus_diffusion"] = _event_ms(learned, reps)
-    # the network evaluated in the diffusion prologue (features + fallback + fused diffusion)
-    r["ms_fused_learned_diffusion"] = _event_ms(lambda: diffusion_learned(mlp, dev, out_l, nu_lb, flag_b), reps)
+    # the one-call entry point (the same kernels as learned())
+    r["ms_learned_diffusion_call"] = _event_ms(lambda: diffusion_learned(mlp, dev, out_l, nu_lb, flag_b), reps)
     return r
 
 

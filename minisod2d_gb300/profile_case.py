@@ -7,9 +7,10 @@ Builds a structured mesh (``--nx``^3 hexes, ``--jitter``) with seeded fields
 (``--kind`` 0 smooth, 1 shock-like), then runs each selected kernel
 ``--warmup`` + ``--iters`` times in order.  Kernels: convec, diffu,
 convec_mixed, diffu_mixed (``--precision`` fp16 / bf16), estimator (plain
-entropy viscosity), learned (features + network + fallback, with a freshly
-initialised network unless ``--weights`` names a weight file), diffu_learned
-(the diffusion with the network in its prologue; needs ``--weights``),
+entropy viscosity), learned (features with the network + fallback, with a
+freshly initialised network unless ``--weights`` names a weight file),
+diffu_learned (the same followed by the per-element-viscosity diffusion;
+needs ``--weights``),
 diffu_nu (the diffusion with one viscosity per element),
 tet_convec / tet_diffu (fem_convec / fem_diffu on the reference driver's
 disconnected tetrahedra over the case's nodes).

@@ -239,7 +239,7 @@ def test_shipped_network_on_held_out_combined_96_seed(cuda):
 
 
 def _learned_from_T(m, dev):
-    """The separate-kernel path on the same inputs as the fused one (p = rho Rgas T)."""
+    """msod_learned_viscosity on the inputs of diffusion_learned(from_T=True) (p = rho Rgas T)."""
     import torch
 
     nu = torch.empty(dev.nelem, device=dev.rho.device)
@@ -250,9 +250,9 @@ def _learned_from_T(m, dev):
     return nu, flag
 
 
-def test_fused_network_in_diffusion_prologue_equals_separate_kernels(cuda):
-    """The network evaluated in the diffusion prologue gives the viscosity of the
-    separate prediction kernel and the same residuals.  (Not bit for bit: the
+def test_learned_diffusion_call_equals_separate_calls(cuda):
+    """msod_diffusion_ijk_learned gives the viscosity of msod_learned_viscosity and
+    the residuals of msod_diffusion_ijk_nu with it.  (Not bit for bit: the
     entropy normalisation n_eta comes from an FP64 atomic sum over the nodes,
     so two runs of either path differ in the last bits.)"""
     import torch
@@ -265,7 +265,7 @@ def test_fused_network_in_diffusion_prologue_equals_separate_kernels(cuda):
     learn.diffusion_ijk_nu(dev, nu_ref, ref)
     out = [torch.empty_like(x) for x in ref]
     _, nu, flag = learn.diffusion_learned(m, dev, out, from_T=True)
-    print("FUSED fallback %d of %d" % (int(flag.sum()), dev.nelem))
+    print("LEARNED fallback %d of %d" % (int(flag.sum()), dev.nelem))
     assert torch.equal(flag, flag_ref)
     a, b = nu.cpu().numpy(), nu_ref.cpu().numpy()
     assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30)) < 1e-5
@@ -273,8 +273,8 @@ def test_fused_network_in_diffusion_prologue_equals_separate_kernels(cuda):
         assert refimpl.rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
 
 
-def test_fused_network_fallback(cuda):
-    """Every element outside the training range: the fused path uses the plain estimator."""
+def test_learned_diffusion_fallback(cuda):
+    """Every element outside the training range: the one-call path uses the plain estimator."""
     import torch
 
     host, dev = _dev(cuda, 4, 3, seed=4)
@@ -297,27 +297,37 @@ def test_fused_network_fallback(cuda):
     assert refimpl.rel_l2(nu.cpu().numpy(), nu_p.cpu().numpy()) < 1e-5
 
 
-def test_fused_network_without_fallback(cuda):
-    """No element falls back (unbounded training ranges): every viscosity comes
-    from the network evaluated in the prologue and matches the prediction kernel."""
+@pytest.mark.parametrize("P", [2, 4, 5, 7])
+def test_learned_viscosity_matches_prediction_on_features(cuda, P):
+    """No element falls back (unbounded training ranges): the viscosity of
+    msod_learned_viscosity equals msod_mlp_predict on the features of
+    msod_mlp_features (the same fields), for trained weights (the shipped 48^3
+    network) and for freshly initialised ones, at orders whose feature kernels
+    differ in block shape."""
     import torch
 
-    host, dev = _dev(cuda, 4, 5, seed=6)
-    m = learn.Mlp(seed=3)
-    w, norm = m.params()
-    norm = norm.copy()
-    norm[24:36] = -1e30
-    norm[36:48] = 1e30
-    m.set_params(None, norm)
-    nu_ref, flag_ref = _learned_from_T(m, dev)
-    _, nu, flag = learn.diffusion_learned(m, dev, from_T=True)
-    assert int(flag.sum()) == 0 and int(flag_ref.sum()) == 0
-    a, b = nu.cpu().numpy(), nu_ref.cpu().numpy()
-    assert np.all(a > 0)
-    assert np.max(np.abs(a - b) / np.abs(b)) < 1e-5
+    host, dev = _dev(cuda, P, 4, seed=6)
+    shipped = learn.Mlp()
+    shipped.load(learn.shipped_weights("learned_48"))
+    for m in (learn.Mlp(seed=3), shipped):
+        w, norm = m.params()
+        norm = norm.copy()
+        norm[24:36] = -1e30
+        norm[36:48] = 1e30
+        m.set_params(None, norm)
+        nu, flag = learn.learned_viscosity(m, dev)
+        feat, numax = learn.features(dev)
+        _, nu_ref, _ = m.predict(feat, numax)
+        ref = nu_ref.cpu().numpy()
+        a = nu.cpu().numpy()
+        assert int(flag.sum()) == 0
+        assert np.all(a > 0)
+        d = np.abs(a - ref) / np.abs(ref)
+        print("LEARNED-NU P=%d max rel diff %.2e, identical %d of %d" % (P, d.max(), int((a == ref).sum()), a.size))
+        assert d.max() < 1e-5
 
 
-def test_fused_network_with_pressure_matches_separate_path(cuda):
+def test_learned_diffusion_with_pressure_matches_separate_calls(cuda):
     """With the pressure itself (as the separate path takes it) the shipped
     network needs no fallback on its own workload's fields.  (Pressure rebuilt
     as rho Rgas T carries rounding noise where the training fields have an

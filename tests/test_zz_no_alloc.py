@@ -74,16 +74,26 @@ import numpy as np, torch
 dev = torch.device("cuda:0")
 P = 4
 t = fem.element_tables(P)
-con, _, nelem, npoin = fem.structured_mesh(P, 3, 3, 3, t, 0.0, 0, coords=False)
-d = {k: torch.from_numpy(np.ascontiguousarray(t[k])).to(dev) for k in ("dlxigp_ip", "invAtoIJK", "AtoI", "AtoJ", "AtoK")}
+con, coord, nelem, npoin = fem.structured_mesh(P, 3, 3, 3, t, 0.0, 0)
+d = {k: torch.from_numpy(np.ascontiguousarray(t[k])).to(dev)
+     for k in ("dlxigp_ip", "invAtoIJK", "AtoI", "AtoJ", "AtoK", "dNgp", "wgp")}
 connec = torch.from_numpy(con).to(dev)
 args = [P, nelem, npoin] + [C.c_void_p(x.data_ptr()) for x in (connec, d["dlxigp_ip"], d["invAtoIJK"], d["AtoI"],
                                                                d["AtoJ"], d["AtoK"])] + [None]
-# One kernel launch and one device-to-host copy before the measured window: the driver sets up
-# per-context state at the first launch (8 MiB on this GPU, the size of the default device-side
-# malloc heap), which belongs to no library call.
-warm = torch.ones(4, device=dev).add_(1.0).sum().item()
+# Before the measured window, one launch of another kernel of the library that allocates
+# nothing (elem_jacobian into torch buffers): the driver sets up state of its own at the first
+# launch from the library's module (8 MiB on this GPU), which belongs to no library call.
+n = (P + 1) ** 3
+d_coord = torch.from_numpy(coord).to(dev)
+He = torch.empty(9 * nelem * n, device=dev)
+gp = torch.empty(nelem * n, device=dev)
 torch.cuda.synchronize()
+free_w0 = torch.cuda.mem_get_info()[0]
+assert L.msod_elem_jacobian(P, nelem, npoin, C.c_void_p(connec.data_ptr()), C.c_void_p(d_coord.data_ptr()),
+                            C.c_void_p(d["dNgp"].data_ptr()), C.c_void_p(d["wgp"].data_ptr()),
+                            C.c_void_p(gp.data_ptr()), C.c_void_p(He.data_ptr()), None) == 0
+torch.cuda.synchronize()
+print("WARMUP first launch from the library's module took %%d bytes" %% (free_w0 - torch.cuda.mem_get_info()[0]))
 free0 = torch.cuda.mem_get_info()[0]
 rcs = [L.msod_check_element_tables_noalloc(*args) for _ in range(5)]
 torch.cuda.synchronize()
@@ -96,13 +106,14 @@ print("RESULT", rcs, free0, free1, rc_alloc, free2)
 
 
 def test_noalloc_allocates_nothing_in_a_fresh_process(cuda):
-    """In a fresh process whose only library calls are the allocation-free entry point (inputs
-    built by torch, the library's module loaded eagerly with the context, the context's first
-    kernel launch done by torch beforehand), five calls leave the device's free memory
-    unchanged."""
+    """In a fresh process (inputs built by torch, the library's module loaded eagerly with the
+    context, one launch of another allocation-free library kernel beforehand), five calls of the
+    allocation-free entry point -- the first with its per-device set-up included -- leave the
+    device's free memory unchanged."""
     env = dict(os.environ, CUDA_MODULE_LOADING="EAGER")
     out = subprocess.run([sys.executable, "-c", FRESH], capture_output=True, text=True, env=env, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
+    print("\n".join(x for x in out.stdout.splitlines() if x.startswith("WARMUP")))
     line = [x for x in out.stdout.splitlines() if x.startswith("RESULT")][-1]
     rcs, rest = line[len("RESULT "):].split("]")
     assert [int(x) for x in rcs.strip(" [").split(",")] == [capi.MSOD_OK] * 5
