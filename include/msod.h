@@ -436,8 +436,8 @@ int msod_diffusion_ijk_nu(int porder, int nelem, int npoin, const int *connec, c
  *              caller's FP32 arrays.
  *   mu_e_mode  MSOD_MU_E_GIVEN: the caller's mu_e (default); MSOD_MU_E_PLAIN:
  *              the entropy-viscosity estimator; MSOD_MU_E_LEARNED: the
- *              network `mlp` (in the FP32 diffusion's prologue) with the
- *              estimator as per-element fallback.  Both ignore the mu_e
+ *              network `mlp` (msod_learned_viscosity) with the estimator
+ *              as per-element fallback.  Both ignore the mu_e
  *              argument and use p = rho Rgas Tem, gamma = 1.4, Rgas = 287
  *              (main.f90:52), ce = 0.1, cmax = 0.5 (mod_numerical_params.f90:23-24).
  * The network is kept by reference and must outlive its use.  The library

@@ -146,7 +146,7 @@ int mode_diffusion(int porder, int nelem, int npoin, const int *connec, const fl
     const msod_mlp *mlp = g_mlp.load();
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (nelem < 1 || npoin < 1 || !rho || !Tem) return set_error(MSOD_ERR_INVALID_ARG, "bad sizes or NULL field");
-    // The network in the FP32 diffusion's prologue.
+    // FP32 with the network: the one-call learned diffusion.
     if (mue == MSOD_MU_E_LEARNED && prec == MSOD_PREC_FP32)
         return msod_diffusion_ijk_learned(mlp, porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK,
                                           gmshAtoI, gmshAtoJ, gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_sgs, Tem,
