@@ -326,25 +326,48 @@ constexpr size_t diffu_smem_bytes()
            (size_t)(DIFFU_NBUF * G::NPL + 2 * G::N) * sizeof(int);
 }
 
-// Threads per line of the FP32 diffusion (0: the line-geometry default, one).
-// Measured on 64^3 hexes: porder 4 is fastest with one (1.84 ms; 2.08-2.27 ms
-// with 2, 3 or 5: more warps, but the line loads are repeated per thread).
-// Porder 5 with one and the fused zeta stage, three elements per 128-thread
-// block: 2.97 ms, against 3.78 ms with two threads per line (three elements per
-// 224-thread block, unfused) and 3.19 ms with one at two elements per block.
+// Threads per line of the FP32 diffusion (0: the line-geometry default: one
+// up to porder 5, two at 6-7, three at 8; one is the only form with the fused
+// zeta stage).  Measured on 64^3 hexes: porder 4
+// is fastest with one (1.84 ms; 2.08-2.27 ms with 2, 3 or 5: more warps, but
+// the line loads are repeated per thread).  Porder 5 with one and the fused
+// zeta stage, three elements per 128-thread block: 2.97 ms, against 3.78 ms
+// with two threads per line (three elements per 224-thread block, unfused) and
+// 3.19 ms with one at two elements per block.  Porder 7 on 32^3 hexes with one
+// and the fused zeta stage, two elements per 128-thread block (161 registers):
+// 1.183 ms, against 1.266 ms with two (unfused, 256 threads), 1.345 ms with one
+// element and 1.255 ms with three per block.  Porder 6 on 32^3 hexes with one,
+// three elements per 160-thread block: 0.685 ms, against 0.787 ms with two
+// (0.687 ms at two elements).  Porder 8 on 32^3 hexes keeps three: 1.907 ms,
+// against 2.20 / 2.13 ms with one at one / two elements per block.
 #ifndef DIFFU_S4
 #define DIFFU_S4 0
 #endif
 #ifndef DIFFU_S5
 #define DIFFU_S5 1
 #endif
+#ifndef DIFFU_S6
+#define DIFFU_S6 1
+#endif
+#ifndef DIFFU_S7
+#define DIFFU_S7 1
+#endif
+#ifndef DIFFU_S8
+#define DIFFU_S8 0
+#endif
 template <typename real, int P>
 constexpr int diffu_s()
 {
-    return sizeof(real) == 4 ? (P == 4 ? DIFFU_S4 : (P == 5 ? DIFFU_S5 : 0)) : 0;
+    return sizeof(real) != 4 ? 0
+           : P == 4          ? DIFFU_S4
+           : P == 5          ? DIFFU_S5
+           : P == 6          ? DIFFU_S6
+           : P == 7          ? DIFFU_S7
+           : P == 8          ? DIFFU_S8
+                             : 0;
 }
 
-// Elements per block of the FP32 porder-4 / porder-5 diffusion (0: the
+// Elements per block of the FP32 diffusion at porders 4-8 (0: the
 // line-geometry default).
 #ifndef DIFFU_NE4
 #define DIFFU_NE4 0
@@ -352,13 +375,26 @@ constexpr int diffu_s()
 #ifndef DIFFU_NE5
 #define DIFFU_NE5 3
 #endif
+#ifndef DIFFU_NE6
+#define DIFFU_NE6 3
+#endif
+#ifndef DIFFU_NE7
+#define DIFFU_NE7 2
+#endif
+#ifndef DIFFU_NE8
+#define DIFFU_NE8 0
+#endif
 template <typename real, int P>
 constexpr int diffu_necap()
 {
-    return (sizeof(real) == 4 && P == 4 && DIFFU_NE4 > 0)   ? DIFFU_NE4
-           : (sizeof(real) == 4 && P == 5 && DIFFU_NE5 > 0) ? DIFFU_NE5
-                                                             : necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES,
-                                                                         (int)sizeof(real), 200 * 1024);
+    constexpr int ne = sizeof(real) != 4 ? 0
+                       : P == 4          ? DIFFU_NE4
+                       : P == 5          ? DIFFU_NE5
+                       : P == 6          ? DIFFU_NE6
+                       : P == 7          ? DIFFU_NE7
+                       : P == 8          ? DIFFU_NE8
+                                         : 0;
+    return ne > 0 ? ne : necap_for(2 * NDF + 3 * NX, LineGeom<real, P>::ES, (int)sizeof(real), 200 * 1024);
 }
 
 template <typename real, int P>

@@ -138,14 +138,19 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
         usum += um; csum += c;
         spdmax = fmaxf(spdmax, um + c);
     }
+    // Warp minima / maxima as one reduction each on order-preserving integer
+    // keys (the two non-negative ones on their bits); sums by butterfly, which
+    // leaves the same value on every lane.
+    auto wmin = [](float v) { return key2f(__reduce_min_sync(~0u, f2key(v))); };
+    auto wmax = [](float v) { return key2f(__reduce_max_sync(~0u, f2key(v))); };
+    rmin = wmin(rmin); rmax = wmax(rmax);
+    pmin = wmin(pmin); pmax = wmax(pmax);
+    smin = wmin(smin); smax = wmax(smax);
+    emin = wmin(emin); emax = wmax(emax);
+    machmax = __uint_as_float(__reduce_max_sync(~0u, __float_as_uint(machmax)));
+    spdmax = __uint_as_float(__reduce_max_sync(~0u, __float_as_uint(spdmax)));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        rmin = fminf(rmin, __shfl_xor_sync(~0u, rmin, o)); rmax = fmaxf(rmax, __shfl_xor_sync(~0u, rmax, o));
-        pmin = fminf(pmin, __shfl_xor_sync(~0u, pmin, o)); pmax = fmaxf(pmax, __shfl_xor_sync(~0u, pmax, o));
-        smin = fminf(smin, __shfl_xor_sync(~0u, smin, o)); smax = fmaxf(smax, __shfl_xor_sync(~0u, smax, o));
-        emin = fminf(emin, __shfl_xor_sync(~0u, emin, o)); emax = fmaxf(emax, __shfl_xor_sync(~0u, emax, o));
-        machmax = fmaxf(machmax, __shfl_xor_sync(~0u, machmax, o));
-        spdmax = fmaxf(spdmax, __shfl_xor_sync(~0u, spdmax, o));
         rsum += __shfl_xor_sync(~0u, rsum, o); psum += __shfl_xor_sync(~0u, psum, o);
         usum += __shfl_xor_sync(~0u, usum, o); csum += __shfl_xor_sync(~0u, csum, o);
         vol += __shfl_xor_sync(~0u, vol, o);
@@ -176,7 +181,7 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
             const int a = node(I, J, K);
             const float r = sv[w][0][a], pr = sv[w][1][a];
             rv[k] = r;
-            ev[k] = r * (logf(pr) - gamma * logf(r)) / (gamma - 1.0f);
+            ev[k] = r * ((log2_approx(pr) - gamma * log2_approx(r)) * s_scale);
             uv[k] = sv[w][2 + d][a];
         }
         d2r_l = fabsf(rv[0] - 2.f * rv[1] + rv[2]);
@@ -200,12 +205,15 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
         d2e = fmaxf(d2e, __shfl_sync(~0u, d2e_l, 9 + d));
         defect = fmaxf(defect, __shfl_sync(~0u, def_l, 9 + d));
     }
-    if (lane != 0) return;
+    // Every lane holds the element's reductions; lane k < 12 forms feature k
+    // (one division and at most one logarithm per lane) and the twelve lanes
+    // store the element's features together.
     const double mean = esum / (double)npoin;
     const double lo = (double)key2f(ekmin), hi = (double)key2f(ekmax);
     float neta = (float)fmax(hi - mean, mean - lo);
     if (!(neta > 0.0f)) neta = 1.0f;
-    const float rmean = rsum / N, pmean = psum / N, umean = usum / N, cmean = csum / N;
+    constexpr float invN = 1.0f / (float)N;
+    const float rmean = rsum * invN, pmean = psum * invN, umean = usum * invN, cmean = csum * invN;
     const float h = cbrtf(vol) / (float)P;
     float G[3][3];  // G[i][j] = d u_i / d x_j = sum_k He(j,k) gi[i][k]
     for (int i = 0; i < 3; ++i)
@@ -218,20 +226,22 @@ __global__ void __launch_bounds__(32 * feat_warps<P>())
             const float sij = 0.5f * (G[i][j] + G[j][i]);
             s2 += sij * sij;
         }
-    const float sc = h / cmean;
-    float *f = feat + (size_t)e * kMlpIn;
-    f[0] = flog((rmax - rmin) / rmean);
-    f[1] = flog((pmax - pmin) / pmean);
-    f[2] = flog(smax - smin);
-    f[3] = umean / cmean;
-    f[4] = machmax;
-    f[5] = theta * sc;
-    f[6] = flog(sqrtf(w0 * w0 + w1 * w1 + w2 * w2) * sc);
-    f[7] = flog(sqrtf(s2) * sc);
-    f[8] = flog(d2r / rmean);
-    f[9] = flog(d2e / neta);
-    f[10] = flog((emax - emin) / neta);
-    f[11] = flog(defect / (neta * (umean + cmean)));
+    // Feature k = num / den, through flog except features 3, 4 and 5.
+    float num = rmax - rmin, den = rmean;                              // 0
+    if (lane == 1) { num = pmax - pmin; den = pmean; }
+    if (lane == 2) { num = smax - smin; den = 1.0f; }
+    if (lane == 3) { num = umean; den = cmean; }
+    if (lane == 4) { num = machmax; den = 1.0f; }
+    if (lane == 5) { num = theta * h; den = cmean; }
+    if (lane == 6) { num = sqrtf(w0 * w0 + w1 * w1 + w2 * w2) * h; den = cmean; }
+    if (lane == 7) { num = sqrtf(s2) * h; den = cmean; }
+    if (lane == 8) { num = d2r; den = rmean; }
+    if (lane == 9) { num = d2e; den = neta; }
+    if (lane == 10) { num = emax - emin; den = neta; }
+    if (lane == 11) { num = defect; den = neta * (umean + cmean); }
+    const float v = num / den;
+    if (lane < kMlpIn) feat[(size_t)e * kMlpIn + lane] = (lane >= 3 && lane <= 5) ? v : flog(v);
+    if (lane != 0) return;
     if (numax_out) numax_out[e] = cmax * h * spdmax;
 }
 
