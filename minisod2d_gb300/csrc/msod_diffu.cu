@@ -66,6 +66,14 @@
 #ifndef DIFFU_LINEMAP
 #define DIFFU_LINEMAP 4
 #endif
+// Where the map applies: 0 = never, 1 = always, 2 = on meshes whose elements
+// share nodes (npoin < nelem * nodes per element), not on disconnected ones.
+// Measured through the driver, porder 4 (on / off): disconnected meshes of
+// 192,000 and 262,144 hexes 1.043 / 1.018 and 1.404 / 1.373 ms; structured
+// 64^3 and 48^3 meshes 1.323 / 1.373 and 0.585 / 0.604 ms.
+#ifndef DIFFU_LINEMAP_MODE
+#define DIFFU_LINEMAP_MODE 2
+#endif
 // Gather of the node fields: 0 = 4-byte cp.async copies, 1 = loads into
 // registers, then 32-lane shared-memory stores.  Measured: plain_64 1.466
 // against 1.483 ms (at three blocks per SM, DIFFU_MINB4=3), porder 5 on 64^3
@@ -77,14 +85,13 @@
 namespace msod {
 namespace {
 
-// The thread's line in direction dir.
+// The thread's line in direction dir (linemap: the launch's choice of map).
 template <class G>
-__device__ __forceinline__ LineThread<G> diffu_line(int tid, int dir)
+__device__ __forceinline__ LineThread<G> diffu_line(int tid, int dir, int linemap)
 {
     if constexpr (G::P <= DIFFU_LINEMAP && G::S == 1)
-        return LineThread<G>(kLineMap<G>.code[dir][tid], true);
-    else
-        return LineThread<G>(tid);
+        if (linemap) return LineThread<G>(kLineMap<G>.code[dir][tid], true);
+    return LineThread<G>(tid);
 }
 
 __constant__ float c_Df[MSOD_MAX_PORDER + 1][kTableDMax];
@@ -413,7 +420,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                  const typename G::real *__restrict__ Tem, const typename G::real *__restrict__ mu_fluid,
                  const typename G::real *__restrict__ mu_e, const typename G::real *__restrict__ mu_sgs,
                  const typename G::real *__restrict__ nu_elem, typename G::real *__restrict__ Rmass,
-                 typename G::real *__restrict__ Rmom, typename G::real *__restrict__ Rener)
+                 typename G::real *__restrict__ Rmom, typename G::real *__restrict__ Rener, int linemap)
 {
     using real = typename G::real;
     constexpr int Q = G::Q, N = G::N, QP = G::QP, ES = G::ES, NE = G::NE, NT = G::NT, NPL = G::NPL;
@@ -432,7 +439,8 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     int *sLat = sPerm + N;
 
     const int tid = threadIdx.x;
-    const LineThread<G> lt0 = diffu_line<G>(tid, 0), lt1 = diffu_line<G>(tid, 1), lt2 = diffu_line<G>(tid, 2);
+    const LineThread<G> lt0 = diffu_line<G>(tid, 0, linemap), lt1 = diffu_line<G>(tid, 1, linemap),
+                        lt2 = diffu_line<G>(tid, 2, linemap);
     constexpr bool FUSEZ = diffu_fusez<G>();
     constexpr bool LATE = FUSEZ && DIFFU_HE_LATE != 0;
     constexpr int MP = LATE ? 1 : (FUSEZ ? Q : IPT);  // points whose He and gpvol a thread holds
@@ -789,8 +797,10 @@ cudaError_t launch_diffu_pn(const DiffuArgs<real> &a, const TableScratch *tabs, 
     const int ngroups = (a.nelem + G::NE - 1) / G::NE;
     const int grid = persistent_grid(kern, G::NT, smem, ngroups);
     if (grid <= 0) return cudaErrorInvalidConfiguration;
+    const int linemap = DIFFU_LINEMAP_MODE == 2 ? (a.npoin < (long long)a.nelem * G::N ? 1 : 0) : DIFFU_LINEMAP_MODE;
     kern<<<grid, G::NT, smem, st>>>(a.nelem, a.npoin, ngroups, a.connec, a.He, a.gpvol, tabs, a.Cp, a.Pr, a.rho, a.u,
-                                    a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.nu_elem, a.Rmass, a.Rmom, a.Rener);
+                                    a.Tem, a.mu_fluid, a.mu_e, a.mu_sgs, a.nu_elem, a.Rmass, a.Rmom, a.Rener,
+                                    linemap);
     return cudaGetLastError();
 }
 
