@@ -495,13 +495,20 @@ int main(int argc, char **argv)
         }
     }
 
-    // FP64 check: the FP64 build of the hex calls on the same inputs promoted to
-    // FP64 (mu_e: the caller's, or the plain estimator's when it is estimated).
+    // FP64 check: the FP64 build of the hex calls, with the element tables in
+    // FP64 (as the reference's FP64 build computes them) and the same fields,
+    // He and gpvol promoted to FP64 (mu_e: the caller's, or the plain
+    // estimator's when it is estimated).
     double fe[6] = {0, 0, 0, 0, 0, 0};
     if (o.fp64_check) {
         auto up64 = [&](const std::vector<double> &h) { return upload(h); };
         const std::vector<double> He64 = widen(download(d_He, 9 * ne)), gp64 = widen(download(d_gpvol, ne));
-        double *e_He = up64(He64), *e_gp = up64(gp64), *e_dlx = up64(widen(dlx));
+        std::vector<int> i64(n), a64(n), b64(n), c64(n), k64(n);
+        std::vector<double> x64(3 * n), w64(n), N64((size_t)n * n), dN64(3 * (size_t)n * n), dlx64(3 * (size_t)n * Q);
+        check(msod_fem_element_tables_f64(P, i64.data(), k64.data(), a64.data(), b64.data(), c64.data(), x64.data(),
+                                          w64.data(), N64.data(), dN64.data(), dlx64.data()),
+              "msod_fem_element_tables_f64");
+        double *e_He = up64(He64), *e_gp = up64(gp64), *e_dlx = up64(dlx64);
         double *e_u = up64(widen(u)), *e_q = up64(widen(q)), *e_rho = up64(widen(rho)), *e_pr = up64(widen(pr));
         double *e_E = up64(widen(E)), *e_Tem = up64(widen(Tem)), *e_muf = up64(widen(muf)), *e_mus = up64(widen(mus));
         std::vector<double> mue64;

@@ -1,16 +1,20 @@
 """GPU checks of the mixed-precision convection (FP16 / BF16 hi + lo tensor-core
 contractions, FP64 scatter and energy-flux assembly).
 
-Reference: the FP64 oracle on the same inputs (the FP32 fields and geometry
-the kernel reads, promoted to FP64).  The plain FP32 GPU kernel's distance
-from the same FP64 answer (the FP32 floor) is printed beside each result.
+Reference: the FP64 oracle with the element tables in FP64 (as the
+reference's FP64 build computes them) and the FP32 fields, He and gpvol the
+kernel reads, promoted to FP64.  The plain FP32 GPU kernel's distance from the
+same FP64 answer (the FP32 floor) is printed beside each result.
 Criteria per residual (relative L2):
   * convection: <= 1e-4 for both formats and <= 1e-5 for FP16;
-  * diffusion: <= max(1e-4, 6 x floor) for FP16 and <= max(5e-4, 6 x floor)
-    for BF16.  Its weak divergence cancels strongly between neighbouring
-    elements (the FP32 floor itself reaches 4e-4 for the energy residual of
-    the 32^3 porder-7 workload); the FP16 contractions land at 4-7 x that
-    floor, the BF16 ones (16-bit splits) at 2-4e-4 on these small cases.
+  * diffusion: <= 1e-4 for FP16 and <= max(5e-4, 6 x floor) for BF16.  The
+    weak divergence cancels strongly between neighbouring elements, which
+    magnifies the FP32 rounding of the derivative tables acting on the fields'
+    means in the plain kernel (its floor reaches 2e-3 for the energy residual
+    of the 32^3 porder-7 workload); the mixed kernels contract the fields minus
+    their value at one node of the element, so the rounded tables act on the
+    variation only, and FP16 stays within 1e-4; the BF16 splits (2 x 8
+    significant bits) reach 2-4e-4 on these small cases.
 """
 import numpy as np
 import pytest
@@ -33,9 +37,15 @@ def _case(cuda, P, nx, kind=0, nmodes=8, seed=0, jitter=0.05):
     return host, workload.DeviceCase(host, device=cuda)
 
 
+def _geom64(host, dev):
+    """FP64 element tables (the reference's FP64 build) with the kernel's own He and gpvol."""
+    t64 = O.element_tables(dev.cfg.porder, np.float64)
+    return dict(t64, connec=host.connec, He=dev.He.cpu().numpy().astype(np.float64),
+                gpvol=dev.gpvol.cpu().numpy().astype(np.float64))
+
+
 def _oracle64(host, dev):
-    t = host.tables
-    geom = dict(t, connec=host.connec, He=dev.He.cpu().numpy(), gpvol=dev.gpvol.cpu().numpy())
+    geom = _geom64(host, dev)
     f = host.fields
     return O.full_convec_ijk(dev.cfg.porder, dev.nelem, dev.npoin, geom, f["u"], f["q"], f["rho"], f["pr"], f["E"],
                              dtype=np.float64, nthreads=8)
@@ -114,8 +124,7 @@ def _diffu_case(cuda, P, nx, kind, nmodes, mu=1e-3, seed=0):
 
 
 def _diffu_oracle64(host, dev, mu_e=None):
-    t = host.tables
-    geom = dict(t, connec=host.connec, He=dev.He.cpu().numpy(), gpvol=dev.gpvol.cpu().numpy())
+    geom = _geom64(host, dev)
     f = host.fields
     return O.full_diffusion_ijk(dev.cfg.porder, dev.nelem, dev.npoin, geom, dev.cfg.Cp, dev.cfg.Pr, f["rho"], f["u"],
                                 f["Tem"], f["mu_fluid"], host.mu_e if mu_e is None else mu_e, host.mu_sgs,
@@ -131,10 +140,8 @@ def test_mixed_diffusion_vs_fp64_oracle(cuda, P, nx, kind, nmodes):
         errs = _errs(dev.diffu_mixed(prec), ref)
         print("MIXED-DIFFU P=%d kind=%d %s err=%s floor32=%s" % (
             P, kind, prec, ["%.2e" % x for x in errs], ["%.2e" % x for x in floor]))
-        # The weak divergence cancels strongly between neighbouring elements,
-        # so the diffusion bound is stated against the FP32 floor.
         for name, e, fl in zip(("mass", "mom", "ener"), errs, floor):
-            bound = max(TOL, DIFFU_FLOOR_FACTOR * fl) if prec == "fp16" else max(BF16_DIFFU_TOL, DIFFU_FLOOR_FACTOR * fl)
+            bound = TOL if prec == "fp16" else max(BF16_DIFFU_TOL, DIFFU_FLOOR_FACTOR * fl)
             assert e <= bound, (prec, name, e, fl)
 
 
