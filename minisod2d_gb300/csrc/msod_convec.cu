@@ -74,8 +74,48 @@ __device__ __forceinline__ double cCD<double>(int P, int i)
 #ifndef CONVEC_NE5
 #define CONVEC_NE5 3
 #endif
+// Threads per line of the FP32 convection at porders 6 and 7 (0: the
+// line-geometry default, two) and elements per block there (0: the default).
+// One thread per line lets porder 6 take the compact even-odd pass and
+// porder 7 the packed row-pair passes.  Measured on 32^3 hexes (A/B/A): porder
+// 6 0.823 ms against 1.255 ms with two threads per line (three elements per
+// block: 1.007 ms); porder 7 1.206 ms against 1.390 ms (one element per block:
+// 1.229 ms).
+#ifndef CONVEC_S6
+#define CONVEC_S6 1
+#endif
+#ifndef CONVEC_S7
+#define CONVEC_S7 1
+#endif
+#ifndef CONVEC_NE6
+#define CONVEC_NE6 2
+#endif
+#ifndef CONVEC_NE7
+#define CONVEC_NE7 2
+#endif
+#ifndef CONVEC_S8
+#define CONVEC_S8 0
+#endif
+#ifndef CONVEC_NE8
+#define CONVEC_NE8 0
+#endif
 template <typename real, int P>
-using ConvecGeom = LineGeom<real, P, (sizeof(real) == 4 && P == 5) ? CONVEC_NE5 : 64>;
+constexpr int convec_necap()
+{
+    return sizeof(real) != 4                ? 64
+           : P == 5                         ? CONVEC_NE5
+           : (P == 6 && CONVEC_NE6 > 0)     ? CONVEC_NE6
+           : (P == 7 && CONVEC_NE7 > 0)     ? CONVEC_NE7
+           : (P == 8 && CONVEC_NE8 > 0)     ? CONVEC_NE8
+                                            : 64;
+}
+template <typename real, int P>
+constexpr int convec_s()
+{
+    return sizeof(real) != 4 ? 0 : P == 6 ? CONVEC_S6 : P == 7 ? CONVEC_S7 : P == 8 ? CONVEC_S8 : 0;
+}
+template <typename real, int P>
+using ConvecGeom = LineGeom<real, P, convec_necap<real, P>(), convec_s<real, P>()>;
 
 // Row pairs of the FP32 matrices (packed contractions), per porder:
 // c_CDp[P][(d*Q + c)*H + m] = (D[d][2m][c], D[d][2m+1][c]), H = (Q+1)/2.
@@ -817,6 +857,9 @@ constexpr size_t convec_stage_bytes()
 #ifndef CONVEC_MINB4_STAGED
 #define CONVEC_MINB4_STAGED 3
 #endif
+#ifndef CONVEC_MINB67
+#define CONVEC_MINB67 1
+#endif
 #ifndef CONVEC_MINB4
 #define CONVEC_MINB4 CONVEC_MINB
 #endif
@@ -825,7 +868,9 @@ constexpr int convec_minb()
 {
     using G = ConvecGeom<real, P>;
     return (sizeof(real) == 4 && G::S == 1 && G::NT <= 128 && P >= 3)
-               ? (P == 5 ? CONVEC_MINB5 : (P == 4 ? (convec_staged<real>() ? CONVEC_MINB4_STAGED : CONVEC_MINB4) : CONVEC_MINB))
+               ? (P == 5 ? CONVEC_MINB5
+                         : (P == 4 ? (convec_staged<real>() ? CONVEC_MINB4_STAGED : CONVEC_MINB4)
+                                   : (P >= 6 ? CONVEC_MINB67 : CONVEC_MINB)))
                : 1;
 }
 
