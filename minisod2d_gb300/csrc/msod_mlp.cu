@@ -53,8 +53,25 @@ constexpr int feat_warps()
     return 12288 / (5 * (P + 1) * (P + 1) * (P + 1)) < 8 ? 12288 / (5 * (P + 1) * (P + 1) * (P + 1)) : 8;
 }
 
+// Minimum resident blocks per SM of the features kernel (-1: per porder as
+// measured, the block-size bound alone at the other porders; 0: that bound
+// everywhere).  The kernel waits on its gathers, so residency
+// pays: porder 4 at six 256-thread blocks per SM (40 registers, a 16-byte
+// spill) 0.261 ms for the learned viscosity on 48^3 hexes, against 0.283 ms at
+// five and 0.313 ms at four (the block-size bound, 56-64 registers); porder 5
+// at five (48 registers) 2.69 ms on 96^3 hexes, against 2.87 ms at six and
+// 2.84 ms at four.
+#ifndef FEAT_MINB
+#define FEAT_MINB -1
+#endif
 template <int P>
-__global__ void __launch_bounds__(32 * feat_warps<P>())
+constexpr int feat_minb()
+{
+    return FEAT_MINB >= 0 ? FEAT_MINB : (P == 4 ? 6 : (P == 5 ? 5 : 0));
+}
+
+template <int P>
+__global__ void __launch_bounds__(32 * feat_warps<P>(), feat_minb<P>())
     features_kernel(int nelem, int npoin, const int *__restrict__ connec, const float *__restrict__ He,
                     const float *__restrict__ gpvol, const TableScratch *__restrict__ tabs,
                     const float *__restrict__ rho, const float *__restrict__ u, const float *__restrict__ p_or_T,
