@@ -173,8 +173,24 @@ __device__ __forceinline__ void residual_pass(const LineThread<G> &lt, const flo
     }
 }
 
+// Elements per block at porders 4 and 5 (0: the line-geometry default, five
+// and seven) and minimum resident blocks per SM (0: the block-size bound).
+// Measured (plain estimator, CUDA events): porder 4 on 48^3 hexes 0.398 ms at
+// three elements per 96-thread block against 0.413 ms at five (ten: 0.412 ms);
+// porder 5 on 96^3 hexes 5.78 ms at seven against 5.91 / 6.19 ms at five /
+// three; a minimum of two blocks per SM (more registers) 0.578 / 7.65 ms.
+#ifndef VISC_NE4
+#define VISC_NE4 3
+#endif
+#ifndef VISC_NE5
+#define VISC_NE5 0
+#endif
+#ifndef VISC_MINB
+#define VISC_MINB 0
+#endif
+
 template <class G>
-__global__ void __launch_bounds__(G::NT)
+__global__ void __launch_bounds__(G::NT, VISC_MINB)
     entropy_visc_kernel(int nelem, int npoin, const int *__restrict__ connec, const float *__restrict__ He,
                         const float *__restrict__ gpvol, const float *__restrict__ rho, const float *__restrict__ u,
                         const float *__restrict__ p_or_T, float Rgas, float gamma, float ce, float cmax,
@@ -334,7 +350,7 @@ __global__ void __launch_bounds__(G::NT)
 }
 
 template <int P>
-using ViscGeom = LineGeom<float, P>;
+using ViscGeom = LineGeom<float, P, (P == 4 && VISC_NE4 > 0) ? VISC_NE4 : ((P == 5 && VISC_NE5 > 0) ? VISC_NE5 : 64)>;
 
 // Preferred shared-memory carveout of the porder-5 estimator, percent of the
 // maximum (-1: none). Its 51.5 KB blocks fill a 228 KB carveout four to an SM
