@@ -215,6 +215,48 @@ def cpu_baseline(cfg, host, seconds=15.0):
                       "prorated by element share" % (ne, host.nelem, dt)}
 
 
+def host_link(device, mib=256, reps=4):
+    """This box's pinned-host <-> device copy bandwidth (GB/s): upload alone, download alone,
+    and both at once on two streams (the e2e step's copies overlap like the latter)."""
+    import torch
+
+    n = mib * 1024 * 1024 // 4
+    h_up = torch.ones(n, dtype=torch.float32).pin_memory()
+    h_dn = torch.empty(n, dtype=torch.float32).pin_memory()
+    d_up = torch.empty(n, dtype=torch.float32, device=device)
+    d_dn = torch.ones(n, dtype=torch.float32, device=device)
+    s1, s2 = torch.cuda.Stream(device=device), torch.cuda.Stream(device=device)
+
+    def timed(up, down):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s1)
+        s2.wait_event(a)
+        for _ in range(reps):
+            if up:
+                with torch.cuda.stream(s1):
+                    d_up.copy_(h_up, non_blocking=True)
+            if down:
+                with torch.cuda.stream(s2):
+                    h_dn.copy_(d_dn, non_blocking=True)
+        s1.wait_stream(s2)
+        b.record(s1)
+        b.synchronize()
+        return (int(up) + int(down)) * reps * n * 4 / (a.elapsed_time(b) * 1e6)
+
+    timed(True, True)
+    return {"h2d_gbs": timed(True, False), "d2h_gbs": timed(False, True), "both_gbs": timed(True, True)}
+
+
+def link_floor_ms(h2d, d2h, link):
+    """Least time for a step's copies on this link: both directions share it (both_gbs, split
+    evenly) until the smaller one is done, then the rest of the larger one runs alone."""
+    half = link["both_gbs"] / 2.0
+    small, large = min(h2d, d2h), max(h2d, d2h)
+    alone = link["h2d_gbs"] if h2d >= d2h else link["d2h_gbs"]
+    return (small / half + (large - small) / alone) / 1e6
+
+
 def workload_config(cfg, nelem, npoin):
     """The `config` of both arms' JSON lines: the workload alone (arm details sit outside it)."""
     Bc, Bd = algorithmic_bytes(nelem, cfg.nnode, npoin)
@@ -372,6 +414,7 @@ def run_ours(args, cfg, rank, local, world):
                 capi.check(L.msod_d2h(h.data_ptr(), o.data_ptr(), o.numel() * o.element_size(), s_down.cuda_stream))
             ev_done[b].record(s_down)
 
+        link = host_link(device)
         for k in range(args.warmup):
             e2e_step(k)
         torch.cuda.synchronize()
@@ -389,6 +432,7 @@ def run_ours(args, cfg, rank, local, world):
         e2e_ms = max_over_ranks(a.elapsed_time(b), world, device) / args.steps
         e2e = {"value": world * 5.0 * dev.npoin / (e2e_ms * 1e-3) / 1e9, "unit": "GDOF/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+               "host_link": dict(link, floor_ms_per_step=link_floor_ms(h2d, d2h, link)),
                "path": "per step: msod_h2d x9 (pinned host -> device), msod_convec_ijk, msod_diffusion_ijk, "
                        "msod_d2h x6 (device -> pinned host); steps pipelined over two device buffer sets on three "
                        "streams (uploads of k+1 and downloads of k-1 overlap the kernels of k), fill and drain "
