@@ -655,11 +655,28 @@ def variant_tet(reps, host):
     return res
 
 
+def variant_rk4(reps, host):
+    """rk4_64: one explicit RK4 step (four stages of convection + diffusion through the C ABI, the
+    lumped mass, the stage updates) on the plain_64 state, against four plain steps."""
+    from minisod2d_gb300 import timestep, workload
+
+    dev = workload.DeviceCase(host)
+    Ml = timestep.lumped_mass(dev)
+    ws = timestep.workspace(dev)
+    rho, q, rhoE = dev.rho.clone(), dev.q.clone(), (dev.rho * dev.E).contiguous()
+    t = _ms(lambda: timestep.rk4_step(dev, Ml, 1e-4, rho, q, rhoE, ws), reps)
+    tp = _ms(lambda: (dev.convec(), dev.diffu()), reps)
+    return {"workload": "rk4_64: the plain_64 state (rho, q = rho u, rhoE), dt = 1e-4, mu_e = mu_sgs = 0",
+            "ms_per_step": t, "gdofs": 5.0 * dev.npoin / (t * 1e-3) / 1e9, "four_plain_steps_ms": 4.0 * tp,
+            "stage_overhead_ms": t - 4.0 * tp, "workspace_bytes": int(ws.numel())}
+
+
 def run_variants(reps=10, host=None):
     out = {}
     variants = [("mixed_p7", variant_mixed), ("learned_48", variant_learned), ("combined_96", variant_combined)]
     if host is not None:
         variants.insert(0, ("tet_64", lambda r: variant_tet(r, host)))
+        variants.insert(1, ("rk4_64", lambda r: variant_rk4(r, host)))
     for name, fn in variants:
         import torch
 

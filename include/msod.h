@@ -450,6 +450,36 @@ int msod_diffusion_ijk_nu(int porder, int nelem, int npoin, const int *connec, c
 int msod_set_mode(int precision, int mu_e_mode, const msod_mlp *mlp);
 int msod_get_mode(int *precision, int *mu_e_mode);
 
+/* ---------------------------------------------------------------------------
+ * Time integration around the two residual calls.  The reference names it
+ * (flag_rk_order = 4, flag_solver_type = 1 lumped mass,
+ * mod_numerical_params.f90:8,20) but contains none of it.
+ * ------------------------------------------------------------------------- */
+
+/* Lumped (diagonal) mass matrix of the GLL quadrature: Ml(p) = sum of
+ * gpvol(e, g) over the element points g at node p.  Ml (npoin) is written
+ * (intent(out)).  Device pointers. */
+int msod_lumped_mass(int porder, int nelem, int npoin, const int *connec, const float *gpvol,
+                     float *Ml, void *stream);
+/* Bytes of device workspace msod_rk4_step needs for npoin nodes (26 floats
+ * per node). */
+int msod_rk4_workspace_bytes(int npoin, size_t *bytes);
+/* One classical four-stage Runge-Kutta step of
+ *   dU/dt = -Ml^-1 (R_conv(U) + R_diff(U)),  U = (rho, q = rho u, rhoE),
+ * updating rho (npoin), q (3*npoin, q[c*npoin+p]) and rhoE (npoin) in place.
+ * Each stage derives u = q/rho, E = rhoE/rho (the specific energy the
+ * convection takes), pr = (gamma-1)(rhoE - rho|u|^2/2) and
+ * Tem = pr/(rho Rgas), and calls msod_convec_ijk and msod_diffusion_ijk (in
+ * the form msod_set_mode selects) with mu_fluid (npoin), mu_e and mu_sgs
+ * (nelem*ngaus) as given.  Ml from msod_lumped_mass; workspace: device memory
+ * of at least msod_rk4_workspace_bytes.  Asynchronous on the stream. */
+int msod_rk4_step(int porder, int nelem, int npoin, const int *connec, const float *He,
+                  const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK,
+                  const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK, float Cp, float Pr,
+                  float gamma, float Rgas, const float *Ml, const float *mu_fluid,
+                  const float *mu_e, const float *mu_sgs, float dt, float *rho, float *q,
+                  float *rhoE, void *workspace, size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,6 +44,9 @@ SIGNATURES = {
     "msod_malloc": [C.POINTER(_p), _sz],
     "msod_free": [_p],
     "msod_h2d": [_p, _p, _sz, _p],
+    "msod_lumped_mass": [_i, _i, _i, _p, _p, _p, _p],
+    "msod_rk4_workspace_bytes": [_i, C.POINTER(_sz)],
+    "msod_rk4_step": _GEOM64 + [_f, _f, _f, _f] + [_p] * 4 + [_f] + [_p] * 4 + [_sz, _p],
     "msod_d2h": [_p, _p, _sz, _p],
     "msod_memset": [_p, _i, _sz, _p],
     "msod_stream_synchronize": [_p],

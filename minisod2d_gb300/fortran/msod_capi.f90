@@ -822,5 +822,52 @@ module msod_capi
          type(c_ptr), value :: precision
          type(c_ptr), value :: mu_e_mode
       end function msod_get_mode
+      integer(c_int) function msod_lumped_mass(porder, nelem, npoin, connec, gpvol, Ml, &
+            stream) bind(C, name="msod_lumped_mass")
+         import :: c_int, c_ptr
+         integer(c_int), value :: porder
+         integer(c_int), value :: nelem
+         integer(c_int), value :: npoin
+         type(c_ptr), value :: connec
+         type(c_ptr), value :: gpvol
+         type(c_ptr), value :: Ml
+         type(c_ptr), value :: stream
+      end function msod_lumped_mass
+      integer(c_int) function msod_rk4_workspace_bytes(npoin, bytes) bind(C, name="msod_rk4_workspace_bytes")
+         import :: c_int, c_ptr
+         integer(c_int), value :: npoin
+         type(c_ptr), value :: bytes
+      end function msod_rk4_workspace_bytes
+      integer(c_int) function msod_rk4_step(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, &
+            invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, Cp, Pr, gamma, Rgas, Ml, mu_fluid, mu_e, mu_sgs, &
+            dt, rho, q, rhoE, workspace, workspace_bytes, stream) bind(C, name="msod_rk4_step")
+         import :: c_int, c_ptr, c_float, c_size_t
+         integer(c_int), value :: porder
+         integer(c_int), value :: nelem
+         integer(c_int), value :: npoin
+         type(c_ptr), value :: connec
+         type(c_ptr), value :: He
+         type(c_ptr), value :: gpvol
+         type(c_ptr), value :: dlxigp_ip
+         type(c_ptr), value :: invAtoIJK
+         type(c_ptr), value :: gmshAtoI
+         type(c_ptr), value :: gmshAtoJ
+         type(c_ptr), value :: gmshAtoK
+         real(c_float), value :: Cp
+         real(c_float), value :: Pr
+         real(c_float), value :: gamma
+         real(c_float), value :: Rgas
+         type(c_ptr), value :: Ml
+         type(c_ptr), value :: mu_fluid
+         type(c_ptr), value :: mu_e
+         type(c_ptr), value :: mu_sgs
+         real(c_float), value :: dt
+         type(c_ptr), value :: rho
+         type(c_ptr), value :: q
+         type(c_ptr), value :: rhoE
+         type(c_ptr), value :: workspace
+         integer(c_size_t), value :: workspace_bytes
+         type(c_ptr), value :: stream
+      end function msod_rk4_step
    end interface
 end module msod_capi

@@ -235,6 +235,48 @@ def entropy_viscosity(P, nelem, npoin, geom, rho, u, pr, gamma=1.4, ce=0.1, cmax
 
 
 # ---------------------------------------------------------------------------
+# Time integration around the residuals.  The reference names a classical RK4
+# with a lumped mass matrix (flag_rk_order = 4, flag_solver_type = 1,
+# mod_numerical_params.f90:8,20) without containing either; restated in numpy
+# on the oracle's residuals, as the library defines them (msod_rk.cu).
+# ---------------------------------------------------------------------------
+def lumped_mass(P, nelem, npoin, connec, gpvol, dtype=np.float64):
+    """Ml(p) = sum of gpvol(e, g) over the element points g at node p."""
+    n = (P + 1) ** 3
+    ids = np.asarray(connec).reshape(n, nelem).T.reshape(-1) - 1  # element point (e, a) -> node
+    Ml = np.zeros(npoin, dtype)
+    np.add.at(Ml, ids, np.asarray(gpvol, dtype).reshape(-1))      # gpvol[e*n + a]
+    return Ml
+
+
+def rk4_step(P, nelem, npoin, geom, Cp, Pr, gamma, Rgas, Ml, mu_fluid, mu_e, mu_sgs, dt, rho, q, rhoE,
+             dtype=np.float64, nthreads=1):
+    """One classical RK4 step of dU/dt = -Ml^-1 (R_conv(U) + R_diff(U)), U = (rho, q = rho u, rhoE),
+    the primitive fields derived per stage: u = q/rho, E = rhoE/rho, pr = (gamma-1)(rhoE - rho|u|^2/2),
+    Tem = pr/(rho Rgas).  Returns the new (rho, q, rhoE)."""
+    Ml = np.asarray(Ml, dtype)
+    Ml3 = np.tile(Ml, 3)
+
+    def rhs(r, qq, re):
+        u = qq.reshape(3, npoin) / r
+        E = re / r
+        pr = (gamma - 1.0) * (re - 0.5 * r * (u * u).sum(0))
+        Tem = pr / (r * Rgas)
+        uf = np.ascontiguousarray(u.reshape(-1))
+        cm, cq, ce = full_convec_ijk(P, nelem, npoin, geom, uf, qq, r, pr, E, dtype, nthreads=nthreads)
+        dm, dq, de = full_diffusion_ijk(P, nelem, npoin, geom, Cp, Pr, r, uf, Tem, mu_fluid, mu_e, mu_sgs, dtype,
+                                        nthreads=nthreads)
+        return [-(cm + dm) / Ml, -(cq + dq) / Ml3, -(ce + de) / Ml]
+
+    U0 = [np.asarray(x, dtype).copy() for x in (rho, q, rhoE)]
+    k1 = rhs(*U0)
+    k2 = rhs(*[a + 0.5 * dt * k for a, k in zip(U0, k1)])
+    k3 = rhs(*[a + 0.5 * dt * k for a, k in zip(U0, k2)])
+    k4 = rhs(*[a + dt * k for a, k in zip(U0, k3)])
+    return [a + dt / 6.0 * (x1 + 2.0 * x2 + 2.0 * x3 + x4) for a, x1, x2, x3, x4 in zip(U0, k1, k2, k3, k4)]
+
+
+# ---------------------------------------------------------------------------
 # Linear tetrahedra (elem_tet.f90, quadrature_rules.f90:84-99, mod_mesh.f90:71-126,
 # jacobian_oper.f90:138-267, elem_convec.f90:839-948, elem_diffu.f90:199-317)
 # ---------------------------------------------------------------------------
