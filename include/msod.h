@@ -472,7 +472,8 @@ int msod_rk4_workspace_bytes(int npoin, size_t *bytes);
  * Tem = pr/(rho Rgas), and calls msod_convec_ijk and msod_diffusion_ijk (in
  * the form msod_set_mode selects) with mu_fluid (npoin), mu_e and mu_sgs
  * (nelem*ngaus) as given.  Ml from msod_lumped_mass; workspace: device memory
- * of at least msod_rk4_workspace_bytes.  Asynchronous on the stream. */
+ * of at least msod_rk4_workspace_bytes, 4-byte aligned.  Asynchronous on the
+ * stream. */
 int msod_rk4_step(int porder, int nelem, int npoin, const int *connec, const float *He,
                   const float *gpvol, const float *dlxigp_ip, const int *invAtoIJK,
                   const int *gmshAtoI, const int *gmshAtoJ, const int *gmshAtoK, float Cp, float Pr,

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
 
 #include "msod.h"
 #include "msod_internal.h"
@@ -167,6 +168,8 @@ int msod_rk4_step(int porder, int nelem, int npoin, const int *connec, const flo
     if (!(gamma > 1.0f) || !(Rgas > 0.0f) || !std::isfinite(dt))
         return set_error(MSOD_ERR_INVALID_ARG, "gamma must exceed 1, Rgas be positive and dt finite");
     const size_t np = (size_t)npoin;
+    if (reinterpret_cast<uintptr_t>(workspace) % alignof(float) != 0)
+        return set_error(MSOD_ERR_INVALID_ARG, "workspace is not %zu-byte aligned", alignof(float));
     if (workspace_bytes < sizeof(float) * (size_t)kRkPlanes * np)
         return set_error(MSOD_ERR_INVALID_ARG, "workspace of %zu bytes, %zu needed", workspace_bytes,
                          sizeof(float) * (size_t)kRkPlanes * np);

@@ -139,6 +139,9 @@ def test_rk4_rejects_bad_arguments(cuda):
     with pytest.raises(capi.MsodError) as ei:
         timestep.rk4_step(dev, Ml, float("nan"), rho, q, rhoE, ws)
     assert ei.value.code == capi.MSOD_ERR_INVALID_ARG
+    with pytest.raises(capi.MsodError) as ei:  # a workspace that does not start on a float boundary
+        timestep.rk4_step(dev, Ml, 1e-3, rho, q, rhoE, ws[1:])
+    assert ei.value.code == capi.MSOD_ERR_INVALID_ARG
     n = C.c_size_t(0)
     assert capi.lib().msod_rk4_workspace_bytes(dev.npoin, C.byref(n)) == capi.MSOD_OK
     assert n.value == 26 * 4 * dev.npoin
