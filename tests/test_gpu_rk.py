@@ -145,3 +145,28 @@ def test_rk4_rejects_bad_arguments(cuda):
     n = C.c_size_t(0)
     assert capi.lib().msod_rk4_workspace_bytes(dev.npoin, C.byref(n)) == capi.MSOD_OK
     assert n.value == 26 * 4 * dev.npoin
+
+
+def test_rk4_step_follows_the_mode(cuda):
+    """The stages call the two drop-in entry points, so the form msod_set_mode selects applies:
+    with the FP16 tensor-core kernels the step's increments agree with the FP32 step's to the
+    mixed kernels' accuracy, and differ from them (the other kernels ran)."""
+    from minisod2d_gb300 import kernels
+
+    host, dev = _case(cuda, 4, 3, 0)
+    Ml = timestep.lumped_mass(dev)
+    ws = timestep.workspace(dev)
+    r32, q32, e32 = _state(dev)
+    U0 = [x.clone() for x in (r32, q32, e32)]
+    timestep.rk4_step(dev, Ml, 2e-3, r32, q32, e32, ws)
+    r16, q16, e16 = (x.clone() for x in U0)
+    kernels.set_mode("fp16")
+    try:
+        timestep.rk4_step(dev, Ml, 2e-3, r16, q16, e16, ws)
+    finally:
+        kernels.set_mode("fp32")
+    for name, a, b, u0 in zip(NAMES, (r16, q16, e16), (r32, q32, e32), U0):
+        da, db = (a - u0).double().cpu().numpy(), (b - u0).double().cpu().numpy()
+        e = refimpl.rel_l2(da, db)
+        print("RK4 fp16 vs fp32 %s: %.2e" % (name, e))
+        assert 0.0 < e < 1e-4, (name, e)
