@@ -671,12 +671,61 @@ def variant_rk4(reps, host):
             "stage_overhead_ms": t - 4.0 * tp, "workspace_bytes": int(ws.numel())}
 
 
+def porder_sweep(reps=20, porders=range(1, 9), nodes_1d=256):
+    """Both plain kernels at each porder on a structured mesh of nx = nodes_1d / porder hexes a side
+    (about 16.8 M nodes at every porder, +-5 % jitter, smooth fields): time per call, GDOF/s and the
+    fraction of the HBM copy peak of the compulsory bytes (every input read once, every output
+    written once), and the time of the one-call form (msod_convec_diffusion_ijk).  Every working
+    set is far above L2."""
+    import torch
+
+    from minisod2d_gb300 import workload
+
+    peak, kind = peak_hbm()
+    rows = []
+    for P in porders:
+        nx = int(round(nodes_1d / P))
+        dev = workload.DeviceCase(workload.HostCase(workload.custom(P, nx, 0.05)))
+        cb, db = algorithmic_bytes(dev.nelem, dev.cfg.nnode, dev.npoin)
+        tc, td = _ms(lambda: dev.convec(), reps), _ms(lambda: dev.diffu(), reps)
+        tf = _ms(lambda: dev.convec_diffu(), reps)
+        dofs = 5.0 * dev.npoin
+        rows.append({"porder": P, "nx": nx, "nelem": dev.nelem, "npoin": dev.npoin,
+                     "convec_ms": tc, "diffu_ms": td, "gdofs": dofs / ((tc + td) * 1e-3) / 1e9,
+                     "one_call_ms": tf, "one_call_gdofs": dofs / (tf * 1e-3) / 1e9,
+                     "convec_frac": cb / (tc * 1e-3) / 1e9 / peak, "diffu_frac": db / (td * 1e-3) / 1e9 / peak,
+                     "bytes_per_node": (cb + db) / dev.npoin})
+        del dev
+        torch.cuda.empty_cache()
+    return {"porder_sweep": rows, "peak_gbs": peak, "peak_kind": kind,
+            "workload": "structured hex meshes, nx = round(%d / porder) a side, +-5%% jitter, smooth fields "
+                        "(8 modes), seed 0; FP32; inputs above L2" % nodes_1d}
+
+
+def variant_fused(reps, host):
+    """fused_64: the plain_64 step as the two drop-in calls and as one msod_convec_diffusion_ijk
+    call (one kernel at porder 4), with the agreement of the two forms' residuals."""
+    from minisod2d_gb300 import workload
+
+    dev = workload.DeviceCase(host)
+    ts = _ms(lambda: (dev.convec(), dev.diffu()), reps)
+    sep = [x.clone() for x in dev.convec()] + [x.clone() for x in dev.diffu()]
+    tf = _ms(lambda: dev.convec_diffu(), reps)
+    c, d = dev.convec_diffu()
+    names = ("convec_Rmass", "convec_Rmom", "convec_Rener", "diffu_Rmass", "diffu_Rmom", "diffu_Rener")
+    dofs = 5.0 * dev.npoin
+    return {"workload": "fused_64: the plain_64 inputs", "two_calls_ms": ts, "one_call_ms": tf,
+            "two_calls_gdofs": dofs / (ts * 1e-3) / 1e9, "one_call_gdofs": dofs / (tf * 1e-3) / 1e9,
+            "speedup": ts / tf, "rel_l2_one_vs_two": {k: _rel(a, b) for k, a, b in zip(names, c + d, sep)}}
+
+
 def run_variants(reps=10, host=None):
     out = {}
     variants = [("mixed_p7", variant_mixed), ("learned_48", variant_learned), ("combined_96", variant_combined)]
     if host is not None:
         variants.insert(0, ("tet_64", lambda r: variant_tet(r, host)))
         variants.insert(1, ("rk4_64", lambda r: variant_rk4(r, host)))
+        variants.insert(2, ("fused_64", lambda r: variant_fused(r, host)))
     for name, fn in variants:
         import torch
 
@@ -700,9 +749,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the mixed-precision / learned-viscosity measurements beside the plain step")
+    ap.add_argument("--porder-sweep", action="store_true",
+                    help="only time both plain kernels at porders 1-8 on meshes of about 16.8 M nodes")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # the timing rules ask for at least 3 warm-up steps
     from minisod2d_gb300 import workload
+
+    if args.porder_sweep:
+        print(json.dumps(porder_sweep()))
+        return
 
     cfg = workload.CONFIGS[args.config]
     rank, local, world = dist_setup()

@@ -139,6 +139,26 @@ int msod_diffusion_ijk(int porder, int nelem, int npoin, const int *connec, cons
                        const float *mu_fluid, const float *mu_e, const float *mu_sgs, float *Rmass,
                        float *Rmom, float *Rener, void *stream);
 
+/* Both calls of a step in one: what msod_convec_ijk followed by
+ * msod_diffusion_ijk on the same geometry and state return (the reference
+ * makes the two calls back to back on one mesh and state, main.f90:447,477).
+ * The fields are the convection's (u, q, rho, press = its pr, E) and the diffusion's
+ * (rho, u shared; Tem, mu_fluid, mu_e, mu_sgs); the residuals go to Rmass_c,
+ * Rmom_c, Rener_c (convection) and Rmass_d, Rmom_d, Rener_d (diffusion),
+ * which must be six distinct arrays.  At porder 4 one kernel computes both
+ * from one gather per element group; other porders run the two kernels on
+ * one set of tables.  While msod_set_mode selects another
+ * form, the call makes the two drop-in calls in turn. */
+int msod_convec_diffusion_ijk(int porder, int nelem, int npoin, const int *connec,
+                              const float *Ngp, const float *dNgp, const float *He,
+                              const float *gpvol, const float *dlxigp_ip, const float *xgp,
+                              const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
+                              const int *gmshAtoK, float Cp, float Pr, const float *u,
+                              const float *q, const float *rho, const float *press, const float *E,
+                              const float *Tem, const float *mu_fluid, const float *mu_e,
+                              const float *mu_sgs, float *Rmass_c, float *Rmom_c, float *Rener_c,
+                              float *Rmass_d, float *Rmom_d, float *Rener_d, void *stream);
+
 /* FP64 builds of the same kernels (the reference compiled with rp=8,
  * mod_constants.f90:5): the GPU-side FP64 oracle run. */
 int msod_convec_ijk_f64(int porder, int nelem, int npoin, const int *connec, const double *He,
@@ -469,8 +489,8 @@ int msod_rk4_workspace_bytes(int npoin, size_t *bytes);
  * updating rho (npoin), q (3*npoin, q[c*npoin+p]) and rhoE (npoin) in place.
  * Each stage derives u = q/rho, E = rhoE/rho (the specific energy the
  * convection takes), pr = (gamma-1)(rhoE - rho|u|^2/2) and
- * Tem = pr/(rho Rgas), and calls msod_convec_ijk and msod_diffusion_ijk (in
- * the form msod_set_mode selects) with mu_fluid (npoin), mu_e and mu_sgs
+ * Tem = pr/(rho Rgas), and calls msod_convec_diffusion_ijk (in the form
+ * msod_set_mode selects) with mu_fluid (npoin), mu_e and mu_sgs
  * (nelem*ngaus) as given.  Ml from msod_lumped_mass; workspace: device memory
  * of at least msod_rk4_workspace_bytes, 4-byte aligned.  Asynchronous on the
  * stream. */

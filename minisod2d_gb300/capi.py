@@ -53,6 +53,7 @@ SIGNATURES = {
     "msod_convec_ijk": _GEOM + [_p] * 8 + [_p],
     "msod_convec_ijk_split": _GEOM + [_p] * 8 + [_p],
     "msod_diffusion_ijk": _GEOM + [_f, _f] + [_p] * 9 + [_p],
+    "msod_convec_diffusion_ijk": _GEOM + [_f, _f] + [_p] * 9 + [_p] * 6 + [_p],
     "msod_convec_ijk_f64": _GEOM64 + [_p] * 8 + [_p],
     "msod_convec_ijk_mixed": [_i] + _GEOM64 + [_p] * 8 + [_p],
     "msod_diffusion_ijk_mixed": [_i] + _GEOM64 + [_f, _f] + [_p] * 9 + [_p],

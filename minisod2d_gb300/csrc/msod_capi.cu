@@ -211,6 +211,49 @@ static int diffu_impl(int porder, int nelem, int npoin, const int *connec, const
     return rc;
 }
 
+static int fused_impl(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,
+                      const float *dlx, const int *inv, const int *ai, const int *aj, const int *ak, float Cp,
+                      float Pr, const float *u, const float *q, const float *rho, const float *pr, const float *E,
+                      const float *Tem, const float *mu_fluid, const float *mu_e, const float *mu_sgs,
+                      float *Rmass_c, float *Rmom_c, float *Rener_c, float *Rmass_d, float *Rmom_d,
+                      float *Rener_d, void *stream)
+{
+    clear_error();
+    int rc = check_geometry(porder, nelem, npoin, connec, He, gpvol, dlx, inv, ai, aj, ak);
+    if (rc) return rc;
+    if (!u || !q || !rho || !pr || !E || !Tem || !mu_fluid || !mu_e || !mu_sgs)
+        return set_error(MSOD_ERR_INVALID_ARG, "NULL field array");
+    float *outs[6] = {Rmass_c, Rmom_c, Rener_c, Rmass_d, Rmom_d, Rener_d};
+    for (int i = 0; i < 6; ++i) {
+        if (!outs[i]) return set_error(MSOD_ERR_INVALID_ARG, "NULL residual array");
+        for (int j = 0; j < i; ++j)
+            if (outs[i] == outs[j]) return set_error(MSOD_ERR_INVALID_ARG, "the six residual arrays must be distinct");
+    }
+    if (!(Pr != 0.0f)) return set_error(MSOD_ERR_INVALID_ARG, "Pr must be non-zero");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (checked_mode()) {
+        rc = run_check(porder, nelem, npoin, connec, dlx, inv, ai, aj, ak, st);
+        if (rc) return rc;
+    }
+    TableScratch *tabs = device_tables(porder);
+    if (!tabs) return set_error(MSOD_ERR_CUDA, "could not allocate the element-table area");
+    rc = zero_outputs(Rmass_c, Rmom_c, Rener_c, npoin, st);
+    if (!rc) rc = zero_outputs(Rmass_d, Rmom_d, Rener_d, npoin, st);
+    if (rc) return rc;
+    ConvecArgs<float> c;
+    c.nelem = nelem; c.npoin = npoin; c.connec = connec; c.He = He; c.gpvol = gpvol; c.dlxigp_ip = dlx;
+    c.invAtoIJK = inv; c.AtoI = ai; c.AtoJ = aj; c.AtoK = ak;
+    c.u = u; c.q = q; c.rho = rho; c.pr = pr; c.E = E; c.Rmass = Rmass_c; c.Rmom = Rmom_c; c.Rener = Rener_c;
+    DiffuArgs<float> d;
+    static_cast<ElementArgs<float> &>(d) = c;
+    d.Cp = Cp; d.Pr = Pr; d.rho = rho; d.u = u; d.Tem = Tem; d.mu_fluid = mu_fluid; d.mu_e = mu_e;
+    d.mu_sgs = mu_sgs; d.nu_elem = nullptr; d.Rmass = Rmass_d; d.Rmom = Rmom_d; d.Rener = Rener_d;
+    rc = cuda_status(launch_table_prep<float>(porder, c, tabs, st), "table preparation launch");
+    if (!rc) rc = cuda_status(launch_fused(porder, c, d, tabs, st), "convection + diffusion kernel launch");
+    if (!rc && checked_mode()) rc = check_wait_fault(tabs, st, "convection + diffusion kernel");
+    return rc;
+}
+
 }  // namespace msod
 
 using namespace msod;
@@ -329,6 +372,29 @@ int msod_diffusion_ijk(int porder, int nelem, int npoin, const int *connec, cons
                               gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs, Rmass, Rmom, Rener, stream);
     return diffu_impl<float>(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ,
                              gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs, Rmass, Rmom, Rener, stream);
+}
+
+int msod_convec_diffusion_ijk(int porder, int nelem, int npoin, const int *connec, const float *Ngp,
+                              const float *dNgp, const float *He, const float *gpvol, const float *dlxigp_ip,
+                              const float *xgp, const int *invAtoIJK, const int *gmshAtoI, const int *gmshAtoJ,
+                              const int *gmshAtoK, float Cp, float Pr, const float *u, const float *q,
+                              const float *rho, const float *pr, const float *E, const float *Tem,
+                              const float *mu_fluid, const float *mu_e, const float *mu_sgs, float *Rmass_c,
+                              float *Rmom_c, float *Rener_c, float *Rmass_d, float *Rmom_d, float *Rener_d,
+                              void *stream)
+{
+    if (!mode_is_default_convec() || !mode_is_default_diffusion()) {
+        int rc = msod_convec_ijk(porder, nelem, npoin, connec, Ngp, dNgp, He, gpvol, dlxigp_ip, xgp, invAtoIJK,
+                                 gmshAtoI, gmshAtoJ, gmshAtoK, u, q, rho, pr, E, Rmass_c, Rmom_c, Rener_c, stream);
+        if (rc) return rc;
+        return msod_diffusion_ijk(porder, nelem, npoin, connec, Ngp, dNgp, He, gpvol, dlxigp_ip, xgp, invAtoIJK,
+                                  gmshAtoI, gmshAtoJ, gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_e, mu_sgs,
+                                  Rmass_d, Rmom_d, Rener_d, stream);
+    }
+    (void)Ngp; (void)dNgp; (void)xgp;
+    return fused_impl(porder, nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
+                      Cp, Pr, u, q, rho, pr, E, Tem, mu_fluid, mu_e, mu_sgs, Rmass_c, Rmom_c, Rener_c, Rmass_d,
+                      Rmom_d, Rener_d, stream);
 }
 
 int msod_diffusion_ijk_nu(int porder, int nelem, int npoin, const int *connec, const float *He, const float *gpvol,

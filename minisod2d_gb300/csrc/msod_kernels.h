@@ -105,6 +105,12 @@ template <typename real>
 cudaError_t launch_convec_plain(int porder, const ConvecArgs<real> &a, const TableScratch *tabs, cudaStream_t st);
 template <typename real>
 cudaError_t launch_diffu_plain(int porder, const DiffuArgs<real> &a, const TableScratch *tabs, cudaStream_t st);
+// Both plain FP32 kernels on the same inputs (outputs zeroed by the caller;
+// tables prepared): one kernel where fused_porder(porder), else the two
+// kernels in turn.  The convection and diffusion outputs must not overlap.
+bool fused_porder(int porder);
+cudaError_t launch_fused(int porder, const ConvecArgs<float> &c, const DiffuArgs<float> &d, const TableScratch *tabs,
+                         cudaStream_t st);
 
 // Mixed-precision convection: FP32 fields, FP64 residuals (zeroed by the
 // caller; tables prepared).  precision: MSOD_PREC_FP16 or MSOD_PREC_BF16.

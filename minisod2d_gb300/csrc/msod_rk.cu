@@ -14,9 +14,11 @@
 //   u = q / rho, E = rhoE / rho (the specific energy the convection takes),
 //   pr = (gamma - 1) (rhoE - rho |u|^2 / 2), Tem = pr / (rho Rgas).
 // Both residuals are the weak forms their kernels assemble (test functions on
-// the left), so each enters the update with a minus sign.  The stages call
-// msod_convec_ijk and msod_diffusion_ijk, so the form msod_set_mode selects
-// (precision, artificial viscosity) applies to every stage.
+// the left), so each enters the update with a minus sign.  Each stage calls
+// msod_convec_diffusion_ijk: one kernel for both residuals at porder 4 in the
+// default form, the two drop-in calls msod_convec_ijk and msod_diffusion_ijk
+// otherwise, so the form msod_set_mode selects (precision, artificial
+// viscosity) applies to every stage.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -186,13 +188,10 @@ int msod_rk4_step(int porder, int nelem, int npoin, const int *connec, const flo
     rk_derive_kernel<<<grid, 256, 0, st>>>(npoin, rho, q, rhoE, gamma, Rgas, u, E, pr, Tem);
     if (cuda_status("primitive-field launch")) return MSOD_ERR_CUDA;
     for (int stage = 0; stage < 4; ++stage) {
-        int rc = msod_convec_ijk(porder, nelem, npoin, connec, nullptr, nullptr, He, gpvol, dlxigp_ip, nullptr,
-                                 invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, u, q, rho, pr, E, Rc, Rc + np, Rc + 4 * np,
-                                 stream);
-        if (!rc)
-            rc = msod_diffusion_ijk(porder, nelem, npoin, connec, nullptr, nullptr, He, gpvol, dlxigp_ip, nullptr,
-                                    invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, Cp, Pr, rho, u, Tem, mu_fluid, mu_e,
-                                    mu_sgs, Rd, Rd + np, Rd + 4 * np, stream);
+        int rc = msod_convec_diffusion_ijk(porder, nelem, npoin, connec, nullptr, nullptr, He, gpvol, dlxigp_ip,
+                                           nullptr, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, Cp, Pr, u, q, rho, pr,
+                                           E, Tem, mu_fluid, mu_e, mu_sgs, Rc, Rc + np, Rc + 4 * np, Rd, Rd + np,
+                                           Rd + 4 * np, stream);
         if (rc) return rc;
         rk_stage_kernel<<<grid, 256, 0, st>>>(npoin, Ml, Rc, Rc + np, Rc + 4 * np, Rd, Rd + np, Rd + 4 * np, U0, S,
                                               rho, q, rhoE, dt, stage, gamma, Rgas, u, E, pr, Tem);

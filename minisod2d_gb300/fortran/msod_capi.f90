@@ -178,6 +178,45 @@ module msod_capi
          type(c_ptr), value :: Rener
          type(c_ptr), value :: stream
       end function msod_diffusion_ijk
+
+      integer(c_int) function msod_convec_diffusion_ijk(porder, nelem, npoin, connec, Ngp, dNgp, &
+            He, gpvol, dlxigp_ip, xgp, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, Cp, Pr, u, q, rho, &
+            press, E, Tem, mu_fluid, mu_e, mu_sgs, Rmass_c, Rmom_c, Rener_c, Rmass_d, Rmom_d, Rener_d, &
+            stream) bind(C, name="msod_convec_diffusion_ijk")
+         import :: c_float, c_int, c_ptr
+         integer(c_int), value :: porder
+         integer(c_int), value :: nelem
+         integer(c_int), value :: npoin
+         type(c_ptr), value :: connec
+         type(c_ptr), value :: Ngp
+         type(c_ptr), value :: dNgp
+         type(c_ptr), value :: He
+         type(c_ptr), value :: gpvol
+         type(c_ptr), value :: dlxigp_ip
+         type(c_ptr), value :: xgp
+         type(c_ptr), value :: invAtoIJK
+         type(c_ptr), value :: gmshAtoI
+         type(c_ptr), value :: gmshAtoJ
+         type(c_ptr), value :: gmshAtoK
+         real(c_float), value :: Cp
+         real(c_float), value :: Pr
+         type(c_ptr), value :: u
+         type(c_ptr), value :: q
+         type(c_ptr), value :: rho
+         type(c_ptr), value :: press
+         type(c_ptr), value :: E
+         type(c_ptr), value :: Tem
+         type(c_ptr), value :: mu_fluid
+         type(c_ptr), value :: mu_e
+         type(c_ptr), value :: mu_sgs
+         type(c_ptr), value :: Rmass_c
+         type(c_ptr), value :: Rmom_c
+         type(c_ptr), value :: Rener_c
+         type(c_ptr), value :: Rmass_d
+         type(c_ptr), value :: Rmom_d
+         type(c_ptr), value :: Rener_d
+         type(c_ptr), value :: stream
+      end function msod_convec_diffusion_ijk
       integer(c_int) function msod_convec_ijk_f64(porder, nelem, npoin, connec, He, gpvol, &
             dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, u, q, rho, pr, E, Rmass, Rmom, &
             Rener, stream) bind(C, name="msod_convec_ijk_f64")

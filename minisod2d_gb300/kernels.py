@@ -109,6 +109,29 @@ def full_diffusion_ijk(nelem, npoin, connec, Ngp, dNgp, He, gpvol, dlxigp_ip, xg
         raise TypeError("He must be float32 or float64")
 
 
+def full_convec_diffusion_ijk(nelem, npoin, connec, Ngp, dNgp, He, gpvol, dlxigp_ip, xgp, invAtoIJK, gmshAtoI,
+                              gmshAtoJ, gmshAtoK, Cp, Pr, u, q, rho, pr, E, Tem, mu_fluid, mu_e, mu_sgs, Rmass_c,
+                              Rmom_c, Rener_c, Rmass_d, Rmom_d, Rener_d, stream=None):
+    """full_convec_ijk (elem_convec.f90:198) and full_diffusion_ijk (elem_diffu.f90:10) of the same
+    geometry and state in one call (msod_convec_diffusion_ijk, FP32).  Ngp, dNgp, xgp are ignored."""
+    import torch
+
+    real = He.dtype
+    if real != torch.float32:
+        raise TypeError("He must be float32")
+    P, g = _geometry(nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK, real)
+    n = (P + 1) ** 3
+    f = [_ptr(u, "u", real, 3 * npoin), _ptr(q, "q", real, 3 * npoin), _ptr(rho, "rho", real, npoin),
+         _ptr(pr, "pr", real, npoin), _ptr(E, "E", real, npoin), _ptr(Tem, "Tem", real, npoin),
+         _ptr(mu_fluid, "mu_fluid", real, npoin), _ptr(mu_e, "mu_e", real, nelem * n),
+         _ptr(mu_sgs, "mu_sgs", real, nelem * n)]
+    r = [_ptr(Rmass_c, "Rmass_c", real, npoin), _ptr(Rmom_c, "Rmom_c", real, 3 * npoin),
+         _ptr(Rener_c, "Rener_c", real, npoin), _ptr(Rmass_d, "Rmass_d", real, npoin),
+         _ptr(Rmom_d, "Rmom_d", real, 3 * npoin), _ptr(Rener_d, "Rener_d", real, npoin)]
+    capi.call("msod_convec_diffusion_ijk", P, nelem, npoin, g[0], None, None, g[1], g[2], g[3], None, *g[4:],
+              float(Cp), float(Pr), *f, *r, _stream(stream))
+
+
 def full_convec_ijk_mixed(nelem, npoin, connec, He, gpvol, dlxigp_ip, invAtoIJK, gmshAtoI, gmshAtoJ, gmshAtoK,
                           u, q, rho, pr, E, Rmass, Rmom, Rener, precision="fp16", stream=None):
     """Mixed-precision form of elem_convec.f90:198: FP32 fields, FP64 residuals.

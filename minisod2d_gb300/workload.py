@@ -189,6 +189,16 @@ class DeviceCase:
                                    stream=stream)
         return self.Dmass, self.Dmom, self.Dener
 
+    def convec_diffu(self, stream=None):
+        """Both residuals in one call (msod_convec_diffusion_ijk) into the same arrays as convec and diffu."""
+        from . import kernels
+
+        kernels.full_convec_diffusion_ijk(*self.geometry(), self.cfg.Cp, self.cfg.Pr, self.u, self.q, self.rho,
+                                          self.pr, self.E, self.Tem, self.mu_fluid, self.mu_e, self.mu_sgs,
+                                          self.Rmass, self.Rmom, self.Rener, self.Dmass, self.Dmom, self.Dener,
+                                          stream=stream)
+        return (self.Rmass, self.Rmom, self.Rener), (self.Dmass, self.Dmom, self.Dener)
+
 
 class TetCase:
     """The reference driver's TET04 data (main.f90:365-407) on the GPU.

@@ -148,7 +148,8 @@ def test_rk4_rejects_bad_arguments(cuda):
 
 
 def test_rk4_step_follows_the_mode(cuda):
-    """The stages call the two drop-in entry points, so the form msod_set_mode selects applies:
+    """The stages call msod_convec_diffusion_ijk, which makes the two drop-in calls while a form
+    other than the default is selected, so the form msod_set_mode selects applies:
     with the FP16 tensor-core kernels the step's increments agree with the FP32 step's to the
     mixed kernels' accuracy, and differ from them (the other kernels ran)."""
     from minisod2d_gb300 import kernels
