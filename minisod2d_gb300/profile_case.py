@@ -6,7 +6,7 @@
 Builds a structured mesh (``--nx``^3 hexes, ``--jitter``) with seeded fields
 (``--kind`` 0 smooth, 1 shock-like), then runs each selected kernel
 ``--warmup`` + ``--iters`` times in order.  Kernels: convec, diffu,
-convec_mixed, diffu_mixed (``--precision`` fp16 / bf16), estimator (plain
+convec_diffu (both residuals in one call, msod_convec_diffusion_ijk), convec_mixed, diffu_mixed (``--precision`` fp16 / bf16), estimator (plain
 entropy viscosity), learned (features with the network + fallback, with a
 freshly initialised network unless ``--weights`` names a weight file),
 diffu_learned (the same followed by the per-element-viscosity diffusion;
@@ -50,6 +50,8 @@ def main(argv=None):
             calls.append(lambda: dev.convec())
         elif k == "diffu":
             calls.append(lambda: dev.diffu())
+        elif k == "convec_diffu":
+            calls.append(lambda: dev.convec_diffu())
         elif k in ("convec_mixed", "diffu_mixed"):
             if out64 is None:
                 out64 = tuple(torch.empty(n * dev.npoin, dtype=torch.float64, device=dev.He.device)
