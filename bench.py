@@ -215,46 +215,40 @@ def cpu_baseline(cfg, host, seconds=15.0):
                       "prorated by element share" % (ne, host.nelem, dt)}
 
 
-def host_link(device, mib=256, reps=4):
-    """This box's pinned-host <-> device copy bandwidth (GB/s): upload alone, download alone,
-    and both at once on two streams (the e2e step's copies overlap like the latter)."""
+def host_link(ups, downs, s_up, s_down, reps=3):
+    """This box's pinned-host <-> device link, measured with the e2e step's own copies before its
+    timed region: `ups` and `downs` are (device pointer, host pointer, bytes) triples, issued
+    through msod_h2d / msod_d2h on two streams, uploads alone, downloads alone and both at once
+    (as the pipelined step overlaps them).  Returns GB/s and ms per step's copies; both_ms is the
+    least time of a step's copies, the floor of the e2e step."""
     import torch
 
-    n = mib * 1024 * 1024 // 4
-    h_up = torch.ones(n, dtype=torch.float32).pin_memory()
-    h_dn = torch.empty(n, dtype=torch.float32).pin_memory()
-    d_up = torch.empty(n, dtype=torch.float32, device=device)
-    d_dn = torch.ones(n, dtype=torch.float32, device=device)
-    s1, s2 = torch.cuda.Stream(device=device), torch.cuda.Stream(device=device)
+    from minisod2d_gb300 import capi
+
+    L = capi.lib()
 
     def timed(up, down):
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(s1)
-        s2.wait_event(a)
+        a.record(s_up)
+        s_down.wait_event(a)
         for _ in range(reps):
             if up:
-                with torch.cuda.stream(s1):
-                    d_up.copy_(h_up, non_blocking=True)
+                for d, h, n in ups:
+                    capi.check(L.msod_h2d(d, h, n, s_up.cuda_stream))
             if down:
-                with torch.cuda.stream(s2):
-                    h_dn.copy_(d_dn, non_blocking=True)
-        s1.wait_stream(s2)
-        b.record(s1)
+                for d, h, n in downs:
+                    capi.check(L.msod_d2h(h, d, n, s_down.cuda_stream))
+        s_up.wait_stream(s_down)
+        b.record(s_up)
         b.synchronize()
-        return (int(up) + int(down)) * reps * n * 4 / (a.elapsed_time(b) * 1e6)
+        return a.elapsed_time(b) / reps
 
     timed(True, True)
-    return {"h2d_gbs": timed(True, False), "d2h_gbs": timed(False, True), "both_gbs": timed(True, True)}
-
-
-def link_floor_ms(h2d, d2h, link):
-    """Least time for a step's copies on this link: both directions share it (both_gbs, split
-    evenly) until the smaller one is done, then the rest of the larger one runs alone."""
-    half = link["both_gbs"] / 2.0
-    small, large = min(h2d, d2h), max(h2d, d2h)
-    alone = link["h2d_gbs"] if h2d >= d2h else link["d2h_gbs"]
-    return (small / half + (large - small) / alone) / 1e6
+    bu, bd = sum(n for _, _, n in ups), sum(n for _, _, n in downs)
+    tu, td, tb = timed(True, False), timed(False, True), timed(True, True)
+    return {"h2d_ms": tu, "d2h_ms": td, "both_ms": tb, "h2d_gbs": bu / tu / 1e6, "d2h_gbs": bd / td / 1e6,
+            "both_gbs": (bu + bd) / tb / 1e6}
 
 
 def workload_config(cfg, nelem, npoin):
@@ -414,7 +408,10 @@ def run_ours(args, cfg, rank, local, world):
                 capi.check(L.msod_d2h(h.data_ptr(), o.data_ptr(), o.numel() * o.element_size(), s_down.cuda_stream))
             ev_done[b].record(s_down)
 
-        link = host_link(device)
+        link = host_link([(dins[1][k].data_ptr(), hin[k].data_ptr(), hin[k].numel() * hin[k].element_size())
+                          for k in ins],
+                         [(o.data_ptr(), h.data_ptr(), o.numel() * o.element_size()) for o, h in zip(douts[1], hout)],
+                         s_up, s_down)
         for k in range(args.warmup):
             e2e_step(k)
         torch.cuda.synchronize()
@@ -432,7 +429,7 @@ def run_ours(args, cfg, rank, local, world):
         e2e_ms = max_over_ranks(a.elapsed_time(b), world, device) / args.steps
         e2e = {"value": world * 5.0 * dev.npoin / (e2e_ms * 1e-3) / 1e9, "unit": "GDOF/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-               "host_link": dict(link, floor_ms_per_step=link_floor_ms(h2d, d2h, link)),
+               "host_link": dict(link, floor_ms_per_step=link["both_ms"]),
                "path": "per step: msod_h2d x9 (pinned host -> device), msod_convec_ijk, msod_diffusion_ijk, "
                        "msod_d2h x6 (device -> pinned host); steps pipelined over two device buffer sets on three "
                        "streams (uploads of k+1 and downloads of k-1 overlap the kernels of k), fill and drain "

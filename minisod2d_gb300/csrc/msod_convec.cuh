@@ -797,6 +797,11 @@ __device__ __forceinline__ void convec_dir(const real *sF, real *sA, const real 
                                           Rener);
 }
 
+// He and gpvol of a block's elements prefetched into L2 at the block's start
+// (one bulk prefetch per span, by one thread; 0 = no prefetch).
+#ifndef CONVEC_PREFETCH
+#define CONVEC_PREFETCH 1
+#endif
 // He and gpvol of a block's elements staged in shared memory by bulk copies
 // (the group's spans of He(3,3,ngaus,nelem) and gpvol(ngaus,nelem) are
 // contiguous): 1 = FP32 kernels, 0 = per-point loads from global memory.

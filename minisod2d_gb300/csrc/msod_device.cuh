@@ -258,6 +258,24 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 // threads 0..5 with plain loads.  Returns the bulk bytes the caller's
 // mbar_arrive_expect_tx must announce.  Thread `issuer` issues the copy;
 // dst_base is 16-byte aligned and holds bytes + 32.
+// L2 prefetch of the 16-byte-aligned interior of [p, p + nbytes) by the bulk
+// copy unit (one thread; a hint with nothing to wait for; no byte outside the
+// span is touched).
+__device__ __forceinline__ void prefetch_span_l2(const void *p, size_t nbytes)
+{
+    const size_t a = reinterpret_cast<size_t>(p);
+    const size_t a16 = (a + 15) & ~(size_t)15, e16 = (a + nbytes) & ~(size_t)15;
+    if (a16 < e16)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a16), "r"((unsigned)(e16 - a16))
+                     : "memory");
+}
+
+// L2 prefetch of the sector at p (a hint).
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 struct SpanPlan {
     const char *src;
     unsigned bytes, head, bulk, tail, shift;

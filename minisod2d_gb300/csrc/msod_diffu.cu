@@ -221,6 +221,44 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
         __syncthreads();
         stage(g);
     }
+    // Group g's He and gpvol spans into L2 (one thread), a group ahead of
+    // their loads in the zeta stage.
+    auto prefetch_group = [&](int gg) {
+        if constexpr (DIFFU_PREFETCH != 0 && !STAGED) {
+            if (tid == 0 && gg < ngroups) {
+                const int e0 = gg * NE, e1 = min(e0 + NE, nelem);
+                prefetch_span_l2(He + (size_t)e0 * N * 9, (size_t)(e1 - e0) * N * 9 * sizeof(real));
+                prefetch_span_l2(gpvol + (size_t)e0 * N, (size_t)(e1 - e0) * N * sizeof(real));
+            }
+        }
+    };
+    // Group gg's gathered inputs into L2 (ids: its node ids), a group ahead of
+    // the gather: the node fields of its element points and its mu_e, mu_sgs
+    // rows (N rows of NE consecutive values).
+    auto prefetch_nodes = [&](int gg, const int(&ids_g)[IPT]) {
+        if constexpr (DIFFU_PREFETCH >= 3 && NBUF == 1) {
+            const size_t np = (size_t)npoin;
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const int i = tid + k * NT, v = ids_g[k] - 1;
+                if (i < NE * N && (unsigned)v < (unsigned)npoin) {
+                    prefetch_l2(rho + v);
+                    prefetch_l2(Tem + v);
+                    prefetch_l2(mu_fluid + v);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) prefetch_l2(u + c * np + v);
+                }
+            }
+        }
+        if constexpr (DIFFU_PREFETCH >= 2 && NBUF == 1) {
+            if (tid < N) {
+                const size_t row = (size_t)tid * nelem + (size_t)gg * NE;
+                if (VISC == VISC_MU_E) prefetch_l2(mu_e + row);
+                prefetch_l2(mu_sgs + row);
+            }
+        }
+    };
+    prefetch_group(g);
     int ids[IPT];
     load_ids(g, ids);
     __syncthreads();  // sLat ready
@@ -232,6 +270,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
 
     int s = 0;
     for (; g < ngroups; g = gn, gn += stride, s = NBUF == 2 ? s ^ 1 : 0) {
+        prefetch_group(gn);
         real *sFs = sF + s * NDF * NPL;
         int *sNs = sNode + s * NPL;
         real Hm[MP][9], gv[MP];
@@ -239,6 +278,7 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
         if (NBUF == 2 && gn < ngroups) store_ids(ids, sNode + (s ^ 1) * NPL);
         cp_async_wait_all();
         __syncthreads();
+        if (gn < ngroups) prefetch_nodes(gn, ids);
         if (NBUF == 2 && gn < ngroups) {
             gather(gn, sNode + (s ^ 1) * NPL, sF + (s ^ 1) * NDF * NPL);
             if (gn + stride < ngroups) load_ids(gn + stride, ids);

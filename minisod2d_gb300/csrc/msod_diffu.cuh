@@ -345,6 +345,19 @@ __device__ __forceinline__ void zeta_stage(const LineThread<G> &lt, typename G::
     }
 }
 
+// L2 prefetches a group ahead, while a group is computed: 1 = the next
+// group's He and gpvol spans (one bulk prefetch per span, by one thread);
+// 2 = also its mu_e, mu_sgs rows (N rows of NE values, one prefetch per row
+// each); 3 = also the node fields of its element points (its node ids are in
+// registers by then); 0 = none.  Measured on 64^3 porder-4 hexes: 1.481 ms
+// with none, 1.440 ms with the spans, 1.607 ms with the node fields as well
+// (six scattered prefetches per element point cost more issue slots than the
+// gather latency they hide); porder 5 on 51^3: 1.514 / 1.465 ms, porder 7 on
+// 37^3: 1.922 / 1.838 ms (none / spans).
+#ifndef DIFFU_PREFETCH
+#define DIFFU_PREFETCH 1
+#endif
+
 // He and gpvol of a group staged in shared memory by bulk copies (the group's
 // spans of He(3,3,ngaus,nelem) and gpvol(ngaus,nelem) are contiguous), issued
 // one group ahead: 1 = the fused zeta stage's FP32 kernels, 0 = per-point

@@ -19,7 +19,8 @@
 // on the same lattice, with their flux planes over planes 8-19, and scatter
 // the diffusion residuals.  The group's He, gpvol and connec, which the
 // convection has just read, come to the diffusion from L1 / L2.  The next
-// group's node ids load into registers during the diffusion stages.
+// group's node ids load during the convection passes, and its He and gpvol
+// spans, node fields and viscosity rows are prefetched into L2.
 //
 // The kernel serves porder 4 in FP32 (64^3 hexes: 2.90 ms against 2.97 ms
 // for the two kernels).  Porders 5 and 7 also take the same element groups in
@@ -74,6 +75,13 @@ constexpr bool fusable()
 // holds the kernel to two blocks per SM, as the register file does.
 #ifndef FUSED_MINB4
 #define FUSED_MINB4 3
+#endif
+// L2 prefetches a group ahead: 1 = the next group's He and gpvol spans; 2 =
+// also its mu_e, mu_sgs rows; 3 = also the node fields of its element points;
+// 0 = none.  Measured on 64^3 hexes: 2.876 / 2.857 / 3.17 ms (none / spans /
+// spans, rows and node fields).
+#ifndef FUSED_PREFETCH
+#define FUSED_PREFETCH 1
 #endif
 #ifndef FUSED_MINB5
 #define FUSED_MINB5 3
@@ -171,9 +179,47 @@ __global__ void __launch_bounds__(FusedDiffuGeom<P>::NT, fused_minb<P>())
         cp_async_commit();
     };
 
+    // Group gg's He and gpvol spans into L2 (one thread), a group ahead of
+    // their loads in the passes.
+    auto prefetch_group = [&](int gg) {
+        if (FUSED_PREFETCH != 0 && tid == 0 && gg < ngroups) {
+            const int e0 = gg * NE, e1 = min(e0 + NE, nelem);
+            prefetch_span_l2(He + (size_t)e0 * N * 9, (size_t)(e1 - e0) * N * 9 * sizeof(float));
+            prefetch_span_l2(gpvol + (size_t)e0 * N, (size_t)(e1 - e0) * N * sizeof(float));
+        }
+    };
+    int ids[IPT];
+    // The next group's gathered inputs into L2 (ids holds its node ids), during
+    // the diffusion stages: its node fields and its mu_e, mu_sgs rows.
+    auto prefetch_nodes = [&](int gg) {
+        if (FUSED_PREFETCH >= 3) {
+            const size_t np = (size_t)npoin;
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const int i = tid + k * NT, v = ids[k] - 1;
+                if (i < NE * N && (unsigned)v < (unsigned)npoin) {
+                    prefetch_l2(rho + v);
+                    prefetch_l2(Tem + v);
+                    prefetch_l2(mu_fluid + v);
+                    prefetch_l2(pr + v);
+                    prefetch_l2(E + v);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        prefetch_l2(u + c * np + v);
+                        prefetch_l2(q + c * np + v);
+                    }
+                }
+            }
+        }
+        if (FUSED_PREFETCH >= 2 && tid < N) {
+            const size_t row = (size_t)tid * nelem + (size_t)gg * NE;
+            prefetch_l2(mu_e + row);
+            prefetch_l2(mu_sgs + row);
+        }
+    };
     int g = blockIdx.x;
     const int stride = gridDim.x;
-    int ids[IPT];
+    prefetch_group(g);
     load_ids(g, ids);
     __syncthreads();  // sLat ready
     store_ids(ids);
@@ -181,8 +227,10 @@ __global__ void __launch_bounds__(FusedDiffuGeom<P>::NT, fused_minb<P>())
     gather(g);
 
     for (int gn = g + stride; g < ngroups; g = gn, gn += stride) {
+        prefetch_group(gn);
         cp_async_wait_all();
         __syncthreads();
+        if (gn < ngroups) load_ids(gn, ids);
         const int e0 = g * NE;
         // Convection: three line passes, the last one scatters.
         if constexpr (convec_compact_capable<float, P>()) {
@@ -206,9 +254,7 @@ __global__ void __launch_bounds__(FusedDiffuGeom<P>::NT, fused_minb<P>())
                                                         Rmass_c, Rmom_c, Rener_c);
         }
         __syncthreads();
-        // The next group's node ids load during the diffusion stages (not
-        // across the convection passes, whose registers they would take).
-        if (gn < ngroups) load_ids(gn, ids);
+        if (gn < ngroups) prefetch_nodes(gn);
         // Diffusion: xi and eta derivatives, the zeta stage (zeta derivatives,
         // point pass, zeta divergence), the xi and eta divergence passes.
         const LineThread<GD> lt0 = diffu_line<GD>(tid, 0, linemap), lt1 = diffu_line<GD>(tid, 1, linemap),

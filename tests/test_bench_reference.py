@@ -31,18 +31,3 @@ def test_reference_arm_loads_no_product_library():
     assert "PRODUCT_NOT_LOADED" in out.stdout
     assert "ORACLE_LOADED" in out.stdout
     assert "'workload': 'custom_p4_n3'" in out.stdout
-
-
-def test_host_link_floor():
-    """The e2e step's copy floor: both directions share the link until the smaller transfer is
-    done, then the rest of the larger one runs at its one-way rate."""
-    sys.path.insert(0, ROOT)
-    import bench
-
-    link = {"h2d_gbs": 200.0, "d2h_gbs": 100.0, "both_gbs": 300.0}
-    # 1 GB up, 0.5 GB down: 0.5 GB each at 150 GB/s (3.33 ms), then 0.5 GB up at 200 GB/s (2.5 ms)
-    assert abs(bench.link_floor_ms(1e9, 5e8, link) - (5e8 / 150e6 + 5e8 / 200e6)) < 1e-9
-    # downloads larger: the remainder runs at the download rate
-    assert abs(bench.link_floor_ms(5e8, 1e9, link) - (5e8 / 150e6 + 5e8 / 100e6)) < 1e-9
-    # equal transfers: only the shared phase
-    assert abs(bench.link_floor_ms(1e9, 1e9, link) - 1e9 / 150e6) < 1e-9
