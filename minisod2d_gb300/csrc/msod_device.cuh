@@ -260,14 +260,21 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 // dst_base is 16-byte aligned and holds bytes + 32.
 // L2 prefetch of the 16-byte-aligned interior of [p, p + nbytes) by the bulk
 // copy unit (one thread; a hint with nothing to wait for; no byte outside the
-// span is touched).
+// span is touched).  No memory clobber: the prefetch writes nothing, and a
+// clobber would keep the compiler from moving loads across it.
 __device__ __forceinline__ void prefetch_span_l2(const void *p, size_t nbytes)
 {
     const size_t a = reinterpret_cast<size_t>(p);
     const size_t a16 = (a + 15) & ~(size_t)15, e16 = (a + nbytes) & ~(size_t)15;
     if (a16 < e16)
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a16), "r"((unsigned)(e16 - a16))
-                     : "memory");
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a16), "r"((unsigned)(e16 - a16)));
+}
+
+// He(3,3,ngaus,e) and gpvol(ngaus,e) of element e into L2 (one thread).
+__device__ __forceinline__ void prefetch_element_l2(const float *He, const float *gpvol, int e, int ngaus)
+{
+    prefetch_span_l2(He + (size_t)e * ngaus * 9, (size_t)ngaus * 9 * sizeof(float));
+    prefetch_span_l2(gpvol + (size_t)e * ngaus, (size_t)ngaus * sizeof(float));
 }
 
 // L2 prefetch of the sector at p (a hint).

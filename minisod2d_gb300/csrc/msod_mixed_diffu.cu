@@ -136,6 +136,10 @@ __global__ void __launch_bounds__(kThreads)
 
 #pragma unroll 1
     for (int e = blockIdx.x; e < nelem; e += gridDim.x) {
+        if (MIXED_PREFETCH != 0 && tid == 0) {  // He and gpvol spans into L2, an element ahead
+            if (e == (int)blockIdx.x) prefetch_element_l2(He, gpvol, e, N);
+            if (e + (int)gridDim.x < nelem) prefetch_element_l2(He, gpvol, e + gridDim.x, N);
+        }
         __syncthreads();  // the previous element is done with every shared array
         if (tid < 32) sMax[tid] = 0u;
         const float nue = NUE ? ldg(nu_elem + e) : 0.0f;

@@ -9,6 +9,15 @@
 
 namespace msod {
 
+// L2 prefetch of each element's He and gpvol spans an element ahead in the
+// mixed-precision kernels (1; 0 = none).  Off: measured slower, FP16
+// convection / diffusion 6.16 / 4.36 ms against 4.82 / 4.14 ms on 51^3
+// porder-5 hexes, 2.05 / 2.09 against 2.05 / 2.05 ms on 32^3 porder 7 (the
+// plain kernels gain 1-3 % from the same prefetch).
+#ifndef MIXED_PREFETCH
+#define MIXED_PREFETCH 0
+#endif
+
 constexpr int kRowB = 16;  // bytes per half-plane row: 8 halves along i
 
 // One field half of an element: 8 rows per k-plane of the element, 8 Q rows.
