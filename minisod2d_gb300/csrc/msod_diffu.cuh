@@ -350,10 +350,10 @@ __device__ __forceinline__ void zeta_stage(const LineThread<G> &lt, typename G::
 // 2 = also its mu_e, mu_sgs rows (N rows of NE values, one prefetch per row
 // each); 3 = also the node fields of its element points (its node ids are in
 // registers by then); 0 = none.  Measured on 64^3 porder-4 hexes: 1.481 ms
-// with none, 1.440 ms with the spans, 1.607 ms with the node fields as well
-// (six scattered prefetches per element point cost more issue slots than the
-// gather latency they hide); porder 5 on 51^3: 1.514 / 1.465 ms, porder 7 on
-// 37^3: 1.922 / 1.838 ms (none / spans).
+// with none, 1.440 ms with the spans, 1.472 ms with the rows, 1.607 ms with
+// the node fields as well (six scattered prefetches per element point cost
+// more issue slots than the gather latency they hide); porder 5 on 51^3:
+// 1.514 / 1.465 ms, porder 7 on 37^3: 1.922 / 1.838 ms (none / spans).
 #ifndef DIFFU_PREFETCH
 #define DIFFU_PREFETCH 1
 #endif

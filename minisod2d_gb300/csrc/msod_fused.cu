@@ -22,8 +22,8 @@
 // group's node ids load during the convection passes, and its He and gpvol
 // spans, node fields and viscosity rows are prefetched into L2.
 //
-// The kernel serves porder 4 in FP32 (64^3 hexes: 2.90 ms against 2.97 ms
-// for the two kernels).  Porders 5 and 7 also take the same element groups in
+// The kernel serves porder 4 in FP32 (64^3 hexes: 2.88 ms against 2.91 ms
+// for the two kernels, 35 % fewer DRAM reads).  Porders 5 and 7 also take the same element groups in
 // both kernels (one thread per line, NE elements in NT threads), but there
 // the kernel measured slower than the two kernels (FUSED_ALL below); they and
 // the other porders run the two kernels one after the other on the call's
@@ -78,8 +78,8 @@ constexpr bool fusable()
 #endif
 // L2 prefetches a group ahead: 1 = the next group's He and gpvol spans; 2 =
 // also its mu_e, mu_sgs rows; 3 = also the node fields of its element points;
-// 0 = none.  Measured on 64^3 hexes: 2.876 / 2.857 / 3.17 ms (none / spans /
-// spans, rows and node fields).
+// 0 = none.  Measured on 64^3 hexes: 2.876 / 2.857 / 2.898 / 3.17 ms (none /
+// spans / spans and rows / all three).
 #ifndef FUSED_PREFETCH
 #define FUSED_PREFETCH 1
 #endif
