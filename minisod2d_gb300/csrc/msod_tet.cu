@@ -35,6 +35,13 @@
 #ifndef TET_DIFFU_MINB
 #define TET_DIFFU_MINB 4
 #endif
+// L2 prefetch of a block's contiguous element data at its start (one
+// thread), bits: 1 = the convection's He and gpvol spans (4.24 M tets: 0.409
+// against 0.430 ms), 2 = the diffusion's, 4 = the diffusion's mu_e, mu_sgs
+// rows as well (with 2: 0.381 against 0.363 ms, slower).
+#ifndef TET_PREFETCH
+#define TET_PREFETCH 1
+#endif
 
 namespace msod {
 namespace {
@@ -150,6 +157,23 @@ __device__ __forceinline__ void node_values(const real *__restrict__ f, const in
     for (int a = 0; a < 4; ++a) v[a] = ldg(f + ip[a]);
 }
 
+// The block's elements' He(3,3,4) and gpvol(4) spans, and the block's part of
+// the four rows of mu(4, nelem) (mu_e, mu_sgs; may be null), into L2.
+template <typename real>
+__device__ __forceinline__ void prefetch_block_l2(const real *He, const real *gpvol, const real *mu_e,
+                                                  const real *mu_sgs, int nelem)
+{
+    const int e0 = blockIdx.x * blockDim.x, e1 = min(e0 + (int)blockDim.x, nelem);
+    if (e0 >= e1) return;
+    const size_t ne = (size_t)(e1 - e0);
+    prefetch_span_l2(He + (size_t)e0 * 36, ne * 36 * sizeof(real));
+    prefetch_span_l2(gpvol + (size_t)e0 * 4, ne * 4 * sizeof(real));
+    for (int a = 0; a < 4 && mu_e; ++a) {
+        prefetch_span_l2(mu_e + (size_t)a * nelem + e0, ne * sizeof(real));
+        prefetch_span_l2(mu_sgs + (size_t)a * nelem + e0, ne * sizeof(real));
+    }
+}
+
 // gpcar(a, id) = sum_j He(id, j, g) dNgp(j, a, g)   (H = He(:,:,g), He(i,j) at H[j*3+i])
 template <typename real>
 __device__ __forceinline__ void shape_derivatives(const real *H, int g, real (&gpcar)[4][3])
@@ -173,6 +197,7 @@ __global__ void __launch_bounds__(128, TET_CONVEC_MINB)
                       real *__restrict__ Rmass, real *__restrict__ Rmom, real *__restrict__ Rener, int vec_io)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((TET_PREFETCH & 1) && threadIdx.x == 0) prefetch_block_l2<real>(He, gpvol, nullptr, nullptr, nelem);
     if (e >= nelem) return;
     const size_t np = (size_t)npoin;
     int ip[4];
@@ -262,6 +287,8 @@ __global__ void __launch_bounds__(128, TET_DIFFU_MINB)
                      real *__restrict__ Rmom, real *__restrict__ Rener, int vec_io)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((TET_PREFETCH & 2) && threadIdx.x == 0)
+        prefetch_block_l2<real>(He, gpvol, (TET_PREFETCH & 4) ? mu_e : nullptr, mu_sgs, nelem);
     if (e >= nelem) return;
     const size_t np = (size_t)npoin;
     int ip[4];
