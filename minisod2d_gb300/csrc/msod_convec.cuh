@@ -839,8 +839,11 @@ constexpr size_t convec_stage_bytes()
 
 // Blocks per SM the register budget is sized for: four 128-thread blocks (128
 // registers) when the derivative matrices are constant-bank operands; three
-// at porder 4 when He and gpvol are staged (their 25 KB per block leave room
-// for three blocks, so a 128-register budget would buy nothing).
+// at porder 4 (168 registers, no spill): with the group's He prefetched into
+// L2 the fourth block's latency hiding is worth less than the 88-byte spill
+// of a 128-register budget (64^3 hexes: 1.460 against 1.470 ms; 1.508
+// against 1.479 ms before the prefetch); three when He and gpvol are staged
+// (their 25 KB per block leave room for three blocks).
 #ifndef CONVEC_MINB4_STAGED
 #define CONVEC_MINB4_STAGED 3
 #endif
@@ -848,7 +851,7 @@ constexpr size_t convec_stage_bytes()
 #define CONVEC_MINB67 1
 #endif
 #ifndef CONVEC_MINB4
-#define CONVEC_MINB4 CONVEC_MINB
+#define CONVEC_MINB4 3
 #endif
 template <typename real, int P>
 constexpr int convec_minb()
