@@ -333,6 +333,9 @@ cudaError_t launch_convec_p(const ConvecArgs<real> &a, const TableScratch *tabs,
         if (convec_compact_capable<real, P>()) {
             err = cudaMemcpyToSymbolAsync(c_CEO, tabs->EO, sizeof(float) * kTableEOMax, sizeof(float) * kTableEOMax * P,
                                           cudaMemcpyDeviceToDevice, st);
+            if (err == cudaSuccess)
+                err = cudaMemcpyToSymbolAsync(c_CEOp, tabs->EOp, sizeof(float) * kTableEOMax,
+                                              sizeof(float) * kTableEOMax * P, cudaMemcpyDeviceToDevice, st);
             if (err != cudaSuccess) return err;
         }
         if (convec_packed<real, P>()) {

@@ -61,8 +61,11 @@ __device__ __forceinline__ LineThread<G> diffu_line(int tid, int dir, int linema
     return LineThread<G>(tid);
 }
 
+// No FP64 copy under MSOD_FP32_ONLY (see msod_convec.cuh).
 __constant__ float c_Df[MSOD_MAX_PORDER + 1][kTableDMax];
+#ifndef MSOD_FP32_ONLY
 __constant__ double c_Dd[MSOD_MAX_PORDER + 1][kTableDMax];
+#endif
 
 template <typename real>
 __device__ __forceinline__ real cD(int P, int i);
@@ -71,11 +74,13 @@ __device__ __forceinline__ float cD<float>(int P, int i)
 {
     return c_Df[P][i];
 }
+#ifndef MSOD_FP32_ONLY
 template <>
 __device__ __forceinline__ double cD<double>(int P, int i)
 {
     return c_Dd[P][i];
 }
+#endif
 
 enum { D_RHO = 0, D_T, D_U0, D_U1, D_U2, D_MUF, D_MUE, D_MUS, NDF };  // gathered planes
 enum { X_GRHO = 0, X_TAUU, X_GT, X_TAU0, X_TAU1, X_TAU2, NX };        // flux vectors

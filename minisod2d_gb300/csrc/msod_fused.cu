@@ -28,6 +28,11 @@
 // the kernel measured slower than the two kernels (FUSED_ALL below); they and
 // the other porders run the two kernels one after the other on the call's
 // one set of tables.
+// FP32 only: the unit's constant bank holds both kernels' FP32 tables.
+#define MSOD_FP32_ONLY 1
+// Scalar even-odd contractions here (packed: 2.866 against 2.857 ms on 64^3
+// porder-4 hexes).
+#define CONVEC_EO2 0
 #include "msod_convec.cuh"
 #include "msod_diffu.cuh"
 
@@ -314,6 +319,9 @@ cudaError_t launch_fused_p(const ConvecArgs<float> &c, const DiffuArgs<float> &d
                                           cudaMemcpyDeviceToDevice, st);
         if (err == cudaSuccess && convec_compact_capable<float, P>())
             err = cudaMemcpyToSymbolAsync(c_CEO, tabs->EO, sizeof(float) * kTableEOMax,
+                                          sizeof(float) * kTableEOMax * P, cudaMemcpyDeviceToDevice, st);
+        if (err == cudaSuccess && convec_compact_capable<float, P>())
+            err = cudaMemcpyToSymbolAsync(c_CEOp, tabs->EOp, sizeof(float) * kTableEOMax,
                                           sizeof(float) * kTableEOMax * P, cudaMemcpyDeviceToDevice, st);
         if (err == cudaSuccess && convec_packed<float, P>()) {
             constexpr int H = (GC::Q + 1) / 2;

@@ -39,6 +39,9 @@ struct TableScratch {
     float Df[kTableDMax];
     float EO[kTableEOMax];
     int eo_ok;  // 1 when EO represents all three directions' matrices
+    // The even-odd A and B entries side by side, for packed (f32x2)
+    // contractions: EOp[2*(i*M + j)] = A[i][j], EOp[2*(i*M + j) + 1] = B[i][j].
+    alignas(8) float EOp[kTableEOMax];
     double Dd[kTableDMax];
     alignas(8) float Dp[kTableDPairMax];
     int perm[kTableNMax];

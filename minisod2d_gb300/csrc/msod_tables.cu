@@ -54,6 +54,8 @@ __global__ void table_prep_kernel(const int *__restrict__ invAtoIJK, const int *
             const int r = sod_left(i / M), c = sod_left(i % M), cm = sod_mirror(Q, c);
             out->EO[i] = 0.5f * (Dv[r * Q + c] - Dv[r * Q + cm]);
             out->EO[M * M + i] = 0.5f * (Dv[r * Q + c] + Dv[r * Q + cm]);
+            out->EOp[2 * i] = out->EO[i];
+            out->EOp[2 * i + 1] = out->EO[M * M + i];
         }
         if (Q % 2 == 1)
             for (int i = threadIdx.x; i < M; i += blockDim.x) {
