@@ -76,6 +76,11 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                         lt2 = diffu_line<G>(tid, 2, linemap);
     constexpr bool FUSEZ = diffu_fusez<G>();
     constexpr bool LATE = FUSEZ && DIFFU_HE_LATE != 0;
+    // The xi and eta passes in even-odd form when the call's tables allow it
+    // (uniform over the grid).
+    constexpr bool EOK = ((DIFFU_EO >> G::P) & 1) != 0 && FUSEZ && sizeof(real) == 4;
+    bool eo = false;
+    if constexpr (EOK) eo = ldg(&tabs->eo_ok) != 0;
     constexpr int MP = LATE ? 1 : (FUSEZ ? Q : IPT);  // points whose He and gpvol a thread holds
     for (int i = tid; i < N; i += NT) {
         sPerm[i] = tabs->perm[i];
@@ -284,8 +289,13 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
             if (gn + stride < ngroups) load_ids(gn + stride, ids);
         }
         if constexpr (FUSEZ) {
-            if (lt0.active) grad_pass<G, 0>(lt0, sFs, sX, sD);
-            if (lt1.active) grad_pass<G, 1>(lt1, sFs, sX, sD);
+            if (eo) {
+                if (lt0.active) grad_pass<G, 0, EOK>(lt0, sFs, sX, sD);
+                if (lt1.active) grad_pass<G, 1, EOK>(lt1, sFs, sX, sD);
+            } else {
+                if (lt0.active) grad_pass<G, 0>(lt0, sFs, sX, sD);
+                if (lt1.active) grad_pass<G, 1>(lt1, sFs, sX, sD);
+            }
             if constexpr (STAGED) {
                 // Bounded wait for group g's spans; every thread learns the outcome.
                 const bool ok = mbar_wait(sBar, phase);
@@ -327,9 +337,15 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
             if constexpr (STAGED) {
                 if (gn < ngroups) stage(gn);  // the spans of the next group, during the divergence
             }
-            if (lt0.active) div_pass<G, 0, false, false>(lt0, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
-            __syncthreads();
-            if (lt1.active) div_pass<G, 1, false, true>(lt1, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            if (eo) {
+                if (lt0.active) div_pass<G, 0, false, false, EOK>(lt0, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+                __syncthreads();
+                if (lt1.active) div_pass<G, 1, false, true, EOK>(lt1, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            } else {
+                if (lt0.active) div_pass<G, 0, false, false>(lt0, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+                __syncthreads();
+                if (lt1.active) div_pass<G, 1, false, true>(lt1, sFs, sX, sD, sNs, npoin, Rmass, Rmom, Rener);
+            }
         } else {
             if (lt0.active) grad_pass<G, 0>(lt0, sFs, sX, sD);
             if (lt1.active) grad_pass<G, 1>(lt1, sFs, sX, sD);
@@ -387,9 +403,17 @@ cudaError_t launch_diffu_pn(const DiffuArgs<real> &a, const TableScratch *tabs, 
     auto kern = diffu_kernel<G, VISC>;
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    if (sizeof(real) == 4)
+    if (sizeof(real) == 4) {
         err = cudaMemcpyToSymbolAsync(c_Df, table_D<float>(tabs), sizeof(float) * 3 * G::Q * G::Q,
                                       sizeof(float) * kTableDMax * P, cudaMemcpyDeviceToDevice, st);
+        constexpr bool eo = ((DIFFU_EO >> P) & 1) != 0 && diffu_fusez<G>();
+        if (err == cudaSuccess && eo)
+            err = cudaMemcpyToSymbolAsync(c_DEO, tabs->EO, sizeof(float) * kTableEOMax,
+                                          sizeof(float) * kTableEOMax * P, cudaMemcpyDeviceToDevice, st);
+        if (err == cudaSuccess && eo)
+            err = cudaMemcpyToSymbolAsync(c_DEOp, tabs->EOp, sizeof(float) * kTableEOMax,
+                                          sizeof(float) * kTableEOMax * P, cudaMemcpyDeviceToDevice, st);
+    }
     else
         err = cudaMemcpyToSymbolAsync(c_Dd, table_D<double>(tabs), sizeof(double) * 3 * G::Q * G::Q,
                                       sizeof(double) * kTableDMax * P, cudaMemcpyDeviceToDevice, st);

@@ -87,9 +87,69 @@ enum { X_GRHO = 0, X_TAUU, X_GT, X_TAU0, X_TAU1, X_TAU2, NX };        // flux ve
 // After the point pass a stage's gathered planes hold: 0 nu_e, 1 kappa_e, 2..6 partial sums.
 enum { P_NUE = 0, P_KAP = 1, P_DR = 2 };
 
+// Even-odd form of the call's 1-D derivative matrix D (TableScratch::EO and
+// EOp, valid when eo_ok), per porder, for the xi and eta passes with one thread
+// per line: with e_j, o_j the sums and differences of mirror-node values,
+// (D v)[L_i] = S_i + T_i and (D v)[s'(L_i)] = S_i - T_i.  D^T, which the
+// divergence passes apply, is centro-antisymmetric as well; its A and B are D's
+// B and A transposed, and its centre row and column are D's centre column and
+// row, so the same tables serve both.
+__constant__ float c_DEO[MSOD_MAX_PORDER + 1][kTableEOMax];
+__constant__ float2 c_DEOp[MSOD_MAX_PORDER + 1][kTableEOMax / 2];
+// Bit P set: the even-odd xi / eta passes at porder P.  Measured (16.8 M-node
+// meshes, even-odd / full matrix): porder 4 1.443 / 1.438 ms, porder 5 1.452 /
+// 1.462 ms, porder 7 1.809 / 1.852 ms.  The two forms round differently, and
+// the diffusion's cancellation magnifies it: 1.1e-3 apart on plain_64's energy
+// residual, each within the FP32 floor of the FP64 answer.
+#ifndef DIFFU_EO
+#define DIFFU_EO ((1 << 5) | (1 << 7))
+#endif
+
+// d = D v (TR = false) or D^T v (TR = true) along one line, FP32, even-odd
+// form; the odd and even sums of a row advance together by packed FMAs.
+template <int P, bool TR>
+__device__ __forceinline__ void eo_line(const float (&v)[P + 1], float (&d)[P + 1])
+{
+    constexpr int Q = P + 1, M = Q / 2, MC = sod_centre(Q);
+    constexpr bool ODD = (Q % 2) == 1;
+    float ev[M > 0 ? M : 1], od[M > 0 ? M : 1];
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        ev[j] = v[sod_left(j)] + v[sod_mirror(Q, sod_left(j))];
+        od[j] = v[sod_left(j)] - v[sod_mirror(Q, sod_left(j))];
+    }
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        // (odd sum S_i, even sum T_i); D: A[i][j] o_j, B[i][j] e_j; D^T: B[j][i] o_j, A[j][i] e_j.
+        const float mid = ODD ? c_DEO[P][2 * M * M + (TR ? M : 0) + i] * v[MC] : 0.0f;
+        float sO, sE;
+        if constexpr (!TR) {
+            float2 s = make_float2(0.0f, mid);
+#pragma unroll
+            for (int j = 0; j < M; ++j) s = __ffma2_rn(c_DEOp[P][i * M + j], make_float2(od[j], ev[j]), s);
+            sO = s.x;
+            sE = s.y;
+        } else {
+            float2 s = make_float2(mid, 0.0f);  // (T_i, S_i)
+#pragma unroll
+            for (int j = 0; j < M; ++j) s = __ffma2_rn(c_DEOp[P][j * M + i], make_float2(ev[j], od[j]), s);
+            sE = s.x;
+            sO = s.y;
+        }
+        d[sod_left(i)] = sO + sE;
+        d[sod_mirror(Q, sod_left(i))] = sO - sE;
+    }
+    if constexpr (ODD) {
+        float sm = 0.0f;
+#pragma unroll
+        for (int j = 0; j < M; ++j) sm = fmaf(c_DEO[P][2 * M * M + (TR ? 0 : M) + j], od[j], sm);
+        d[MC] = sm;
+    }
+}
+
 // Pass 1, direction DIR: iso-parametric derivatives of rho, T, u0..2 at the
 // thread's points, stored to planes sX[DIR*5 + f].
-template <class G, int DIR>
+template <class G, int DIR, bool EO = false>
 __device__ __forceinline__ void grad_pass(const LineThread<G> &lt, const typename G::real *__restrict__ sF,
                                           typename G::real *__restrict__ sX, const typename G::real *__restrict__ sD)
 {
@@ -97,6 +157,19 @@ __device__ __forceinline__ void grad_pass(const LineThread<G> &lt, const typenam
     constexpr int P = G::P, Q = G::Q, QP = G::QP, R = G::R, NPL = G::NPL;
     constexpr int OST = DIR == 0 ? 1 : (DIR == 1 ? QP : Q * QP);
     const int base = lt.el * G::ES + line_off<DIR, Q, QP>(lt.la, lt.lb, 0);
+    if constexpr (EO) {
+        static_assert(G::S == 1 && sizeof(real) == 4, "even-odd passes: FP32, one thread per line");
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            float v[Q], d[Q];
+#pragma unroll
+            for (int c = 0; c < Q; ++c) v[c] = sF[f * NPL + base + c * OST];
+            eo_line<P, false>(v, d);
+#pragma unroll
+            for (int r = 0; r < Q; ++r) sX[(DIR * 5 + f) * NPL + base + r * OST] = d[r];
+        }
+        return;
+    }
     // Several threads per line: the thread's rows of the matrix, in registers
     // for the pass (a per-lane index into the constant bank would serialise).
     real Dr[G::S > 1 ? R : 1][Q];
@@ -124,7 +197,7 @@ __device__ __forceinline__ void grad_pass(const LineThread<G> &lt, const typenam
 
 // Pass 2, direction DIR: weak divergence along the lines with the transposed
 // derivative matrix; partial sums through planes P_DR.. of the stage.
-template <class G, int DIR, bool FIRST, bool LAST>
+template <class G, int DIR, bool FIRST, bool LAST, bool EO = false>
 __device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::real *__restrict__ sF,
                                          const typename G::real *__restrict__ sX, const typename G::real *__restrict__ sD,
                                          const int *__restrict__ sNode, int npoin,
@@ -151,15 +224,22 @@ __device__ __forceinline__ void div_pass(const LineThread<G> &lt, typename G::re
     }
 #pragma unroll
     for (int x = 0; x < NX; ++x) {
-        real v[Q];
+        real v[Q], dT[EO ? Q : 1];
 #pragma unroll
         for (int c = 0; c < Q; ++c) v[c] = sX[(DIR * NX + x) * NPL + base + c * OST];
+        if constexpr (EO) {
+            static_assert(G::S == 1 && sizeof(real) == 4, "even-odd passes: FP32, one thread per line");
+            eo_line<P, true>(v, dT);
+        }
 #pragma unroll
         for (int rr = 0; rr < R; ++rr) {
             real s = (real)0;
+            if constexpr (EO)
+                s = dT[rr];
+            else
 #pragma unroll
-            for (int c = 0; c < Q; ++c)
-                s = fma(G::S == 1 ? cD<real>(P, (DIR * Q + c) * Q + rr) : Dc[G::S == 1 ? 0 : rr][c], v[c], s);
+                for (int c = 0; c < Q; ++c)
+                    s = fma(G::S == 1 ? cD<real>(P, (DIR * Q + c) * Q + rr) : Dc[G::S == 1 ? 0 : rr][c], v[c], s);
             if (x == X_GRHO) acc[rr][0] += s;
             else if (x == X_TAUU) acc[rr][1] += s;
             else if (x == X_GT) acc[rr][1] = fma(kap[rr], s, acc[rr][1]);

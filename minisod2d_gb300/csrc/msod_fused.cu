@@ -129,6 +129,11 @@ __global__ void __launch_bounds__(FusedDiffuGeom<P>::NT, fused_minb<P>())
     const int tid = threadIdx.x;
     bool compact = false;
     if constexpr (convec_compact_capable<float, P>()) compact = ldg(&tabs->eo_ok) != 0;
+    // The diffusion's xi and eta passes in even-odd form, as in the diffusion
+    // kernel, when the call's tables allow it.
+    constexpr bool EOK = ((DIFFU_EO >> P) & 1) != 0;
+    bool eo = false;
+    if constexpr (EOK) eo = ldg(&tabs->eo_ok) != 0;
     for (int i = tid; i < N; i += NT) {
         sPerm[i] = tabs->perm[i];
         sLat[i] = tabs->lat[i];
@@ -264,8 +269,13 @@ __global__ void __launch_bounds__(FusedDiffuGeom<P>::NT, fused_minb<P>())
         // point pass, zeta divergence), the xi and eta divergence passes.
         const LineThread<GD> lt0 = diffu_line<GD>(tid, 0, linemap), lt1 = diffu_line<GD>(tid, 1, linemap),
                              lt2 = diffu_line<GD>(tid, 2, linemap);
-        if (lt0.active) grad_pass<GD, 0>(lt0, sP, sX, nullptr);
-        if (lt1.active) grad_pass<GD, 1>(lt1, sP, sX, nullptr);
+        if (eo) {
+            if (lt0.active) grad_pass<GD, 0, EOK>(lt0, sP, sX, nullptr);
+            if (lt1.active) grad_pass<GD, 1, EOK>(lt1, sP, sX, nullptr);
+        } else {
+            if (lt0.active) grad_pass<GD, 0>(lt0, sP, sX, nullptr);
+            if (lt1.active) grad_pass<GD, 1>(lt1, sP, sX, nullptr);
+        }
         __syncthreads();
         if (lt2.active) {
             const int ee = e0 + lt2.el;
@@ -281,9 +291,17 @@ __global__ void __launch_bounds__(FusedDiffuGeom<P>::NT, fused_minb<P>())
             zeta_stage<GD>(lt2, sP, sX, he_row, mu_at, Cp, Pr);
         }
         __syncthreads();
-        if (lt0.active) div_pass<GD, 0, false, false>(lt0, sP, sX, nullptr, sNode, npoin, Rmass_d, Rmom_d, Rener_d);
-        __syncthreads();
-        if (lt1.active) div_pass<GD, 1, false, true>(lt1, sP, sX, nullptr, sNode, npoin, Rmass_d, Rmom_d, Rener_d);
+        if (eo) {
+            if (lt0.active)
+                div_pass<GD, 0, false, false, EOK>(lt0, sP, sX, nullptr, sNode, npoin, Rmass_d, Rmom_d, Rener_d);
+            __syncthreads();
+            if (lt1.active)
+                div_pass<GD, 1, false, true, EOK>(lt1, sP, sX, nullptr, sNode, npoin, Rmass_d, Rmom_d, Rener_d);
+        } else {
+            if (lt0.active) div_pass<GD, 0, false, false>(lt0, sP, sX, nullptr, sNode, npoin, Rmass_d, Rmom_d, Rener_d);
+            __syncthreads();
+            if (lt1.active) div_pass<GD, 1, false, true>(lt1, sP, sX, nullptr, sNode, npoin, Rmass_d, Rmom_d, Rener_d);
+        }
         __syncthreads();
         if (gn < ngroups) {  // the next group's node ids, then its fields
             store_ids(ids);
@@ -322,6 +340,12 @@ cudaError_t launch_fused_p(const ConvecArgs<float> &c, const DiffuArgs<float> &d
                                           sizeof(float) * kTableEOMax * P, cudaMemcpyDeviceToDevice, st);
         if (err == cudaSuccess && convec_compact_capable<float, P>())
             err = cudaMemcpyToSymbolAsync(c_CEOp, tabs->EOp, sizeof(float) * kTableEOMax,
+                                          sizeof(float) * kTableEOMax * P, cudaMemcpyDeviceToDevice, st);
+        if (err == cudaSuccess && ((DIFFU_EO >> P) & 1) != 0)
+            err = cudaMemcpyToSymbolAsync(c_DEO, tabs->EO, sizeof(float) * kTableEOMax,
+                                          sizeof(float) * kTableEOMax * P, cudaMemcpyDeviceToDevice, st);
+        if (err == cudaSuccess && ((DIFFU_EO >> P) & 1) != 0)
+            err = cudaMemcpyToSymbolAsync(c_DEOp, tabs->EOp, sizeof(float) * kTableEOMax,
                                           sizeof(float) * kTableEOMax * P, cudaMemcpyDeviceToDevice, st);
         if (err == cudaSuccess && convec_packed<float, P>()) {
             constexpr int H = (GC::Q + 1) / 2;
