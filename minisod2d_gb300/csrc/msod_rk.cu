@@ -164,7 +164,10 @@ int msod_rk4_step(int porder, int nelem, int npoin, const int *connec, const flo
                   float *rhoE, void *workspace, size_t workspace_bytes, void *stream)
 {
     clear_error();
+    if (porder < 1 || porder > MSOD_MAX_PORDER) return set_error(MSOD_ERR_PORDER, "porder %d", porder);
     if (nelem < 1 || npoin < 1) return set_error(MSOD_ERR_INVALID_ARG, "nelem and npoin must be positive");
+    const long long nn = (long long)(porder + 1) * (porder + 1) * (porder + 1);
+    if ((long long)nelem * nn >= (1LL << 31)) return set_error(MSOD_ERR_INVALID_ARG, "nelem*nnode exceeds int32");
     if (!Ml || !rho || !q || !rhoE || !workspace)
         return set_error(MSOD_ERR_INVALID_ARG, "NULL mass, state or workspace");
     if (!(gamma > 1.0f) || !(Rgas > 0.0f) || !std::isfinite(dt))

@@ -156,3 +156,42 @@ def test_mode_switch_arguments():
     finally:
         kernels.set_mode()
     assert kernels.get_mode() == ("fp32", "given")
+
+
+def test_one_call_and_time_update_arguments_rejected_on_host(msod_lib):
+    """msod_convec_diffusion_ijk, msod_lumped_mass, msod_rk4_workspace_bytes and msod_rk4_step report
+    argument errors as codes before any device work."""
+    L = capi.lib()
+    d = C.c_void_p(16)
+    geo = [d, None, None, d, d, d, None, d, d, d, d]  # connec, Ngp, dNgp, He, gpvol, dlx, xgp, inv, AtoI/J/K
+    fields = [d] * 9                                   # u, q, rho, pr, E, Tem, mu_fluid, mu_e, mu_sgs
+    outs = [C.c_void_p(16 * (k + 1)) for k in range(6)]
+    rc = L.msod_convec_diffusion_ijk(9, 10, 100, *geo, 1.0, 1.0, *fields, *outs, None)
+    assert rc == capi.MSOD_ERR_PORDER
+    rc = L.msod_convec_diffusion_ijk(4, 10, 100, *geo, 1.0, 0.0, *fields, *outs, None)
+    assert rc == capi.MSOD_ERR_INVALID_ARG  # Pr = 0
+    rc = L.msod_convec_diffusion_ijk(4, 10, 100, *geo, 1.0, 1.0, *fields[:5], None, *fields[6:], *outs, None)
+    assert rc == capi.MSOD_ERR_INVALID_ARG  # NULL Tem
+    alias = outs[:3] + [outs[0]] + outs[4:]
+    rc = L.msod_convec_diffusion_ijk(4, 10, 100, *geo, 1.0, 1.0, *fields, *alias, None)
+    assert rc == capi.MSOD_ERR_INVALID_ARG
+    assert b"distinct" in L.msod_last_error_string()
+
+    assert L.msod_lumped_mass(0, 10, 100, d, d, d, None) == capi.MSOD_ERR_PORDER
+    assert L.msod_lumped_mass(4, 10, 100, d, None, d, None) == capi.MSOD_ERR_INVALID_ARG
+    n = C.c_size_t(0)
+    assert L.msod_rk4_workspace_bytes(0, C.byref(n)) == capi.MSOD_ERR_INVALID_ARG
+    assert L.msod_rk4_workspace_bytes(100, C.byref(n)) == capi.MSOD_OK and n.value == 26 * 4 * 100
+    g64 = [d, d, d, d, d, d, d, d]  # connec, He, gpvol, dlx, inv, AtoI/J/K
+    phys = [1004.5, 0.71, 1.4, 287.0, d, d, d, d]  # Cp, Pr, gamma, Rgas, Ml, mu_fluid, mu_e, mu_sgs
+    ws = C.c_void_p(4096)
+    def step(P=4, nelem=10, dt=1e-3, w=ws, nbytes=n.value, gamma=1.4):
+        ph = list(phys)
+        ph[2] = gamma
+        return L.msod_rk4_step(P, nelem, 100, *g64, *ph, dt, d, d, d, w, nbytes, None)
+    assert step(P=9) == capi.MSOD_ERR_PORDER
+    assert step(nelem=1 << 30) == capi.MSOD_ERR_INVALID_ARG       # nelem*nnode beyond int32
+    assert step(dt=float("nan")) == capi.MSOD_ERR_INVALID_ARG
+    assert step(gamma=1.0) == capi.MSOD_ERR_INVALID_ARG
+    assert step(w=C.c_void_p(4097)) == capi.MSOD_ERR_INVALID_ARG  # not float-aligned
+    assert step(nbytes=n.value - 4) == capi.MSOD_ERR_INVALID_ARG  # too small
