@@ -346,6 +346,13 @@ __device__ __forceinline__ real kappa_e(real muf, real me, real ms, real r, real
     return muf * Cp / Pr + me * Cp / Pr + Cp * r * ms / (real)0.9;
 }
 
+// Zeta-stage He rows in flight two points ahead instead of one at the porders
+// whose bit is set: porder 5 on 51^3 hexes 1.440 against 1.451 ms; porder 4
+// the same either way (1.438 / 1.437 ms), the one-call kernel slower (2.853
+// against 2.844 ms).
+#ifndef DIFFU_HE_AHEAD2
+#define DIFFU_HE_AHEAD2 (1 << 5)
+#endif
 // Zeta stage of the fused form, one thread per zeta line (lt): the zeta
 // derivatives at the line's points (from its nodal values in registers), the
 // point pass there (the xi and eta fluxes go to sX for their divergence
@@ -374,8 +381,11 @@ __device__ __forceinline__ void zeta_stage(const LineThread<G> &lt, typename G::
 #pragma unroll
         for (int k = 0; k < 5; ++k) acc[rr][k] = (real)0;
     }
-    real Hn[9], gpn;
+    // Rows in flight one point ahead, or two (AHEAD2).
+    constexpr bool AHEAD2 = ((DIFFU_HE_AHEAD2 >> G::P) & 1) != 0;
+    real Hn[9], gpn, Hn2[9], gpn2;
     he_row(0, Hn, gpn);
+    if (AHEAD2 && Q > 1) he_row(1, Hn2, gpn2);
 #pragma unroll
     for (int c = 0; c < Q; ++c) {
         const int o = base + c * OST;
@@ -383,7 +393,14 @@ __device__ __forceinline__ void zeta_stage(const LineThread<G> &lt, typename G::
 #pragma unroll
         for (int j = 0; j < 9; ++j) Hc[j] = Hn[j];
         gc = gpn;
-        if (c + 1 < Q) he_row(c + 1, Hn, gpn);
+        if constexpr (AHEAD2) {
+#pragma unroll
+            for (int j = 0; j < 9; ++j) Hn[j] = Hn2[j];
+            gpn = gpn2;
+            if (c + 2 < Q) he_row(c + 2, Hn2, gpn2);
+        } else if (c + 1 < Q) {
+            he_row(c + 1, Hn, gpn);
+        }
         real gi[3][5];
 #pragma unroll
         for (int d = 0; d < 2; ++d)
