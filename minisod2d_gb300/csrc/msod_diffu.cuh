@@ -347,11 +347,12 @@ __device__ __forceinline__ real kappa_e(real muf, real me, real ms, real r, real
 }
 
 // Zeta-stage He rows in flight two points ahead instead of one at the porders
-// whose bit is set: porder 5 on 51^3 hexes 1.440 against 1.451 ms; porder 4
-// the same either way (1.438 / 1.437 ms), the one-call kernel slower (2.853
+// whose bit is set: porder 5 on 51^3 hexes 1.440 against 1.451 ms, porder 7 on
+// 37^3 1.788 against 1.810 ms (32^3: 1.100 against 1.116 ms); porder 4 the
+// same either way (1.438 / 1.437 ms), the one-call kernel slower (2.853
 // against 2.844 ms).
 #ifndef DIFFU_HE_AHEAD2
-#define DIFFU_HE_AHEAD2 (1 << 5)
+#define DIFFU_HE_AHEAD2 ((1 << 5) | (1 << 7))
 #endif
 // Zeta stage of the fused form, one thread per zeta line (lt): the zeta
 // derivatives at the line's points (from its nodal values in registers), the
