@@ -20,14 +20,14 @@
 // the diffusion residuals.  The group's He, gpvol and connec, which the
 // convection has just read, come to the diffusion from L1 / L2.  The next
 // group's node ids load during the convection passes, and its He and gpvol
-// spans, node fields and viscosity rows are prefetched into L2.
+// spans are prefetched into L2.
 //
-// The kernel serves porder 4 in FP32 (64^3 hexes: 2.88 ms against 2.91 ms
-// for the two kernels, 35 % fewer DRAM reads).  Porders 5 and 7 also take the same element groups in
-// both kernels (one thread per line, NE elements in NT threads), but there
-// the kernel measured slower than the two kernels (FUSED_ALL below); they and
-// the other porders run the two kernels one after the other on the call's
-// one set of tables.
+// The kernel serves porder 4 in FP32 (64^3 hexes: 2.85 ms against 2.90 ms
+// for the two kernels, 35 % fewer DRAM reads).  Porders 5 and 7 also take
+// the same element groups in both kernels (one thread per line, NE elements
+// in NT threads), but there the kernel measured slower than the two kernels
+// (FUSED_ALL below); they and the other porders run the two kernels one after
+// the other on the call's one set of tables.
 // FP32 only: the unit's constant bank holds both kernels' FP32 tables.
 #define MSOD_FP32_ONLY 1
 // Scalar even-odd contractions here (packed: 2.866 against 2.857 ms on 64^3
@@ -81,15 +81,15 @@ constexpr bool fusable()
 #ifndef FUSED_MINB4
 #define FUSED_MINB4 3
 #endif
+#ifndef FUSED_MINB5
+#define FUSED_MINB5 3
+#endif
 // L2 prefetches a group ahead: 1 = the next group's He and gpvol spans; 2 =
 // also its mu_e, mu_sgs rows; 3 = also the node fields of its element points;
 // 0 = none.  Measured on 64^3 hexes: 2.876 / 2.857 / 2.898 / 3.17 ms (none /
 // spans / spans and rows / all three).
 #ifndef FUSED_PREFETCH
 #define FUSED_PREFETCH 1
-#endif
-#ifndef FUSED_MINB5
-#define FUSED_MINB5 3
 #endif
 template <int P>
 constexpr int fused_minb()
