@@ -131,6 +131,17 @@ def test_parity_all_porders(cuda, P):
     _compare(dev.diffu(), _oracle_diffu(host, geom), TOL32, "diffu P=%d" % P, _oracle_diffu(host, geom, np.float64))
 
 
+@pytest.mark.parametrize("P,nx", [(1, 40), (6, 10), (7, 9), (8, 6)])
+def test_convec_persistent_groups(cuda, P, nx):
+    """The persistent convection (porders 1, 6, 7 and 8 in FP32) on meshes with more element groups
+    than the grid holds resident blocks (porder 1: 64,000 elements in groups of 32; 6: 1,000 in
+    pairs; 7: 729 in pairs; 8: 216, one per group), so that every block loops over groups."""
+    host, dev = _case(cuda, P, nx, jitter=0.05, kind=1, seed=P + 20)
+    geom = _geom_host(dev)
+    _compare(dev.convec(), _oracle_convec(host, geom), TOL32, "convec persistent P=%d" % P,
+             _oracle_convec(host, geom, np.float64))
+
+
 @pytest.mark.parametrize("P", [2, 4, 7])
 def test_parity_fp64(cuda, P):
     import torch
