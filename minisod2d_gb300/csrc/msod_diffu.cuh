@@ -98,7 +98,7 @@ __constant__ float c_DEO[MSOD_MAX_PORDER + 1][kTableEOMax];
 __constant__ float2 c_DEOp[MSOD_MAX_PORDER + 1][kTableEOMax / 2];
 // Bit P set: the even-odd xi / eta passes at porder P.  Measured (16.8 M-node
 // meshes, even-odd / full matrix): porder 4 1.443 / 1.438 ms, porder 5 1.452 /
-// 1.462 ms, porder 7 1.809 / 1.852 ms.  The two forms round differently, and
+// 1.462 ms, porder 6 1.543 / 1.550 ms (not set), porder 7 1.809 / 1.852 ms.  The two forms round differently, and
 // the diffusion's cancellation magnifies it: 1.1e-3 apart on plain_64's energy
 // residual, each within the FP32 floor of the FP64 answer.
 #ifndef DIFFU_EO
@@ -350,7 +350,7 @@ __device__ __forceinline__ real kappa_e(real muf, real me, real ms, real r, real
 // whose bit is set: porder 5 on 51^3 hexes 1.440 against 1.451 ms, porder 7 on
 // 37^3 1.788 against 1.810 ms (32^3: 1.100 against 1.116 ms); porder 4 the
 // same either way (1.438 / 1.437 ms), the one-call kernel slower (2.853
-// against 2.844 ms).
+// against 2.844 ms), porder 6 within 0.4 % (1.544 against 1.550 ms; not set).
 #ifndef DIFFU_HE_AHEAD2
 #define DIFFU_HE_AHEAD2 ((1 << 5) | (1 << 7))
 #endif
