@@ -88,21 +88,49 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     }
     if (G::S > 1)
         for (int i = tid; i < 3 * Q * Q; i += NT) sD[i] = table_D<real>(tabs)[i];
-    auto load_ids = [&](int g, int (&ids)[IPT]) {
+    // Group-invariant parts of the gathers (GOFF), per item k of the thread: the
+    // lattice offset of its point in the node-field gather (go), and for the
+    // element-layout loads (node ids, mu_e, mu_sgs) the row offset a nelem + el
+    // (mr) and the element el in bits 20.. of mo, whose low bits take the
+    // lattice offset el ES + lat(a) once sLat is in shared memory; -1 for no item.
+    constexpr bool GOFF = ((DIFFU_GOFF >> G::P) & 1) != 0 && NBUF == 1 && DIFFU_GATHER_LDG == 0;
+    constexpr int KG = GOFF ? IPT : 1;
+    int go[KG], mr[KG], mo[KG];
+    if constexpr (GOFF) {
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
             const int i = tid + k * NT;
-            const int el = i % NE, a = i / NE, e = g * NE + el;
-            ids[k] = (i < NE * N && e < nelem) ? ldg(connec + (size_t)a * nelem + e) : 0;
+            const bool in = i < NE * N;
+            const int el = i / N, l = i - el * N;
+            const int I = l % Q, J = (l / Q) % Q, K = l / (Q * Q);
+            go[k] = in ? el * ES + (K * Q + J) * QP + I : -1;
+            const int el2 = i % NE, a = i / NE;
+            mr[k] = in ? a * nelem + el2 : 0;
+            mo[k] = in ? (el2 << 20) : -1;
+        }
+    }
+    auto load_ids = [&](int g, int (&ids)[IPT]) {
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            if constexpr (GOFF) {
+                const bool ok = mo[k] >= 0 && g * NE + (mo[k] >> 20) < nelem;
+                ids[k] = ok ? ldg(connec + (size_t)(mr[k] + g * NE)) : 0;
+            } else {
+                const int i = tid + k * NT;
+                const int el = i % NE, a = i / NE, e = g * NE + el;
+                ids[k] = (i < NE * N && e < nelem) ? ldg(connec + (size_t)a * nelem + e) : 0;
+            }
         }
     };
     auto store_ids = [&](const int (&ids)[IPT], int *dst) {
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
-            const int i = tid + k * NT;
-            if (i < NE * N) {
-                const int v = ids[k] - 1;
-                dst[(i % NE) * ES + sLat[i / NE]] = (v >= 0 && v < npoin) ? v : -1;
+            const int v = ids[k] - 1;
+            if constexpr (GOFF) {
+                if (mo[k] >= 0) dst[mo[k] & 0xFFFFF] = (v >= 0 && v < npoin) ? v : -1;
+            } else {
+                const int i = tid + k * NT;
+                if (i < NE * N) dst[(i % NE) * ES + sLat[i / NE]] = (v >= 0 && v < npoin) ? v : -1;
             }
         }
     };
@@ -146,6 +174,35 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
                 if (VISC == VISC_MU_E) dst[D_MUE * NPL + ow[k]] = w[k][0];
                 dst[D_MUS * NPL + ow[k]] = w[k][1];
             }
+            return;
+        }
+        if constexpr (GOFF) {
+            const size_t np = (size_t)npoin;
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const int o = go[k];
+                if (o >= 0) {
+                    const int p = ids_s[o];
+                    const bool ok = (unsigned)p < (unsigned)npoin;
+                    const size_t pp = ok ? (size_t)p : 0;
+                    cp_async_elem(dst + D_RHO * NPL + o, rho + pp, ok);
+                    cp_async_elem(dst + D_T * NPL + o, Tem + pp, ok);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) cp_async_elem(dst + (D_U0 + c) * NPL + o, u + c * np + pp, ok);
+                    cp_async_elem(dst + D_MUF * NPL + o, mu_fluid + pp, ok);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                if (mo[k] >= 0) {
+                    const bool ok = g * NE + (mo[k] >> 20) < nelem;
+                    const size_t idx = ok ? (size_t)(mr[k] + g * NE) : 0;
+                    const int o = mo[k] & 0xFFFFF;
+                    if (VISC == VISC_MU_E) cp_async_elem(dst + D_MUE * NPL + o, mu_e + idx, ok);
+                    cp_async_elem(dst + D_MUS * NPL + o, mu_sgs + idx, ok);
+                }
+            }
+            cp_async_commit();
             return;
         }
         for (int i = tid; i < NE * N; i += NT) {
@@ -267,6 +324,11 @@ __global__ void __launch_bounds__(G::NT, diffu_minb<G>())
     int ids[IPT];
     load_ids(g, ids);
     __syncthreads();  // sLat ready
+    if constexpr (GOFF) {
+#pragma unroll
+        for (int k = 0; k < IPT; ++k)
+            if (mo[k] >= 0) mo[k] |= (mo[k] >> 20) * ES + sLat[(tid + k * NT) / NE];
+    }
     store_ids(ids, sNode);
     __syncthreads();
     gather(g, sNode, sF);

@@ -330,13 +330,24 @@ constexpr int diffu_xplanes()
 // porder 4 on 64^3). The other kernels take 0, the block-size-only heuristic
 // (a 1 there raised porder 6 from 115 to 154 registers: one block per SM
 // instead of two).
+// Bit P set: the gathers' group-invariant index arithmetic (lattice offsets,
+// element-layout row offsets) computed once per thread, not per group, at
+// three blocks per SM.  Porder 4 on 64^3 hexes: 1.391 against 1.439 ms.
+#ifndef DIFFU_GOFF
+#define DIFFU_GOFF (1 << 4)
+#endif
 #ifndef DIFFU_MINB4
 #define DIFFU_MINB4 1
 #endif
 template <class G>
 constexpr int diffu_minb()
 {
-    return diffu_fusez<G>() ? ((sizeof(typename G::real) == 4 && G::P == 4) ? DIFFU_MINB4 : 1) : 0;
+    // With the gathers' offsets held in registers (DIFFU_GOFF) the compiler would take ~195
+    // registers (two blocks per SM); three blocks are asked for.
+    return diffu_fusez<G>() ? ((sizeof(typename G::real) == 4 && ((DIFFU_GOFF >> G::P) & 1) != 0)
+                                   ? 3
+                                   : ((sizeof(typename G::real) == 4 && G::P == 4) ? DIFFU_MINB4 : 1))
+                            : 0;
 }
 
 // kappa_e at a node (elem_diffu.f90:143-146).
