@@ -332,7 +332,8 @@ constexpr int diffu_xplanes()
 // instead of two).
 // Bit P set: the gathers' group-invariant index arithmetic (lattice offsets,
 // element-layout row offsets) computed once per thread, not per group, at
-// three blocks per SM.  Porder 4 on 64^3 hexes: 1.391 against 1.439 ms.
+// three blocks per SM.  Porder 4 on 64^3 hexes: 1.391 against 1.439 ms;
+// porder 5 on 51^3 1.455 against 1.446 ms (not set); porder 7 spills.
 #ifndef DIFFU_GOFF
 #define DIFFU_GOFF (1 << 4)
 #endif
