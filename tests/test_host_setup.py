@@ -195,3 +195,34 @@ def test_one_call_and_time_update_arguments_rejected_on_host(msod_lib):
     assert step(gamma=1.0) == capi.MSOD_ERR_INVALID_ARG
     assert step(w=C.c_void_p(4097)) == capi.MSOD_ERR_INVALID_ARG  # not float-aligned
     assert step(nbytes=n.value - 4) == capi.MSOD_ERR_INVALID_ARG  # too small
+
+
+def test_python_entry_points_have_no_cpu_path():
+    """The Python mirror of the hot path refuses host tensors (the library has no CPU path) and
+    wrong dtypes or sizes, before any library call."""
+    import torch
+
+    from minisod2d_gb300 import kernels
+
+    P, nelem, npoin = 4, 2, 10
+    n = (P + 1) ** 3
+    f = lambda k, dt=torch.float32: torch.zeros(k, dtype=dt)
+    i = lambda k: torch.ones(k, dtype=torch.int32)
+    geo = (nelem, npoin, i(nelem * n), None, None, f(9 * nelem * n), f(nelem * n), f(3 * n * (P + 1)), None, i(n),
+           i(n), i(n), i(n))
+    fields = (f(3 * npoin), f(3 * npoin), f(npoin), f(npoin), f(npoin))
+    outs = (f(npoin), f(3 * npoin), f(npoin))
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        kernels.full_convec_ijk(*geo, *fields, *outs)
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        kernels.full_diffusion_ijk(*geo, 1004.5, 0.71, f(npoin), f(3 * npoin), f(npoin), f(npoin), f(nelem * n),
+                                   f(nelem * n), *outs)
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        kernels.full_convec_diffusion_ijk(*geo, 1004.5, 0.71, *fields, f(npoin), f(npoin), f(nelem * n),
+                                          f(nelem * n), *outs, f(npoin), f(3 * npoin), f(npoin))
+    with pytest.raises(TypeError, match="float32"):
+        kernels.full_convec_diffusion_ijk(*geo[:5], f(9 * nelem * n, torch.float64), *geo[6:], 1004.5, 0.71,
+                                          *fields, f(npoin), f(npoin), f(nelem * n), f(nelem * n), *outs, f(npoin),
+                                          f(3 * npoin), f(npoin))
+    with pytest.raises(ValueError, match="not \\(porder\\+1\\)\\^3"):
+        kernels.full_convec_ijk(*geo[:10], i(7), *geo[11:], *fields, *outs)
