@@ -322,14 +322,6 @@ constexpr int diffu_xplanes()
 #ifndef DIFFU_HE_LATE
 #define DIFFU_HE_LATE 1
 #endif
-// Minimum blocks per SM in the launch bounds. The kernels with the fused zeta
-// stage take 1, which lets the compiler spend registers (porder 4: 137 / 153 /
-// 153 for the three viscosity sources, porder 5: 159-163); this holds them to
-// three blocks per SM and keeps the L1 that the larger carveout of a fourth
-// block would take (DIFFU_MINB4 = 4, 128 registers: 1.90 ms against 1.50 ms,
-// porder 4 on 64^3). The other kernels take 0, the block-size-only heuristic
-// (a 1 there raised porder 6 from 115 to 154 registers: one block per SM
-// instead of two).
 // Bit P set: the gathers' group-invariant index arithmetic (lattice offsets,
 // element-layout row offsets) computed once per thread, not per group, at
 // three blocks per SM.  Porder 4 on 64^3 hexes: 1.391 against 1.439 ms;
@@ -337,14 +329,22 @@ constexpr int diffu_xplanes()
 #ifndef DIFFU_GOFF
 #define DIFFU_GOFF (1 << 4)
 #endif
+// Minimum blocks per SM in the launch bounds. The kernels with the fused zeta
+// stage take 1, which lets the compiler spend registers (porder 4 without the
+// gather offsets: 137 / 153 / 153 for the three viscosity sources; porder 5:
+// 159-163); shared memory holds them to three blocks per SM and keeps the L1
+// that the larger carveout of a fourth block would take (DIFFU_MINB4 = 4, 128
+// registers: 1.90 ms against 1.50 ms, porder 4 on 64^3).  With the gather
+// offsets (DIFFU_GOFF) they take 3: left free, the compiler would spend ~195
+// registers (two blocks per SM).  The other kernels take 0, the
+// block-size-only heuristic (a 1 there raised porder 6 from 115 to 154
+// registers: one block per SM instead of two).
 #ifndef DIFFU_MINB4
 #define DIFFU_MINB4 1
 #endif
 template <class G>
 constexpr int diffu_minb()
 {
-    // With the gathers' offsets held in registers (DIFFU_GOFF) the compiler would take ~195
-    // registers (two blocks per SM); three blocks are asked for.
     return diffu_fusez<G>() ? ((sizeof(typename G::real) == 4 && ((DIFFU_GOFF >> G::P) & 1) != 0)
                                    ? 3
                                    : ((sizeof(typename G::real) == 4 && G::P == 4) ? DIFFU_MINB4 : 1))
